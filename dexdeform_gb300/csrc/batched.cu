@@ -1,0 +1,691 @@
+// batched.cu -- the batched MLS-MPM substep and its adjoint for sm_103a.
+//
+// Work decomposition (one launch per phase for all environments):
+//   * particle phases (P2G, G2P, their adjoints): one CTA per tile of
+//     `tile_size` particles of one env (tiles never straddle envs);
+//   * grid phases (grid update and its adjoint): a persistent grid of
+//     `grid_ctas` CTAs walking the active-block list, 64 threads per block.
+// Scatters (P2G and the G2P adjoint) pre-reduce in the warp: lanes are sorted
+// by stencil base cell (a 32-wide bitonic sort on shuffles), equal keys form
+// contiguous segments, each of the 27 node contributions is summed over its
+// segment with five shuffle rounds and the segment head issues one float4
+// vector atomic (red.global.add.v4.f32).  Grids are double-buffered by epoch
+// parity; the grid update of epoch e clears what epoch e-1 touched, so there
+// is no per-substep memset.
+//
+// Arithmetic follows mpm/csrc/integrator.cu (kernels cited per function); the
+// SVD and stress use the cancellation-free forms of mpm_math.cuh.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <climits>
+
+#include "mpm_math.cuh"
+#include "../../include/dexmpm.h"
+
+using namespace dexmpm;
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int PX = 0, PV = 3, PF = 6, PC = 15;  // state plane offsets
+
+__device__ __forceinline__ f3 ldf3(const float *__restrict__ S, int N, int plane, int p) {
+  return mk3(__ldg(S + (size_t)plane * N + p), __ldg(S + (size_t)(plane + 1) * N + p),
+             __ldg(S + (size_t)(plane + 2) * N + p));
+}
+__device__ __forceinline__ void stf3(float *S, int N, int plane, int p, f3 v) {
+  S[(size_t)plane * N + p] = v.x;
+  S[(size_t)(plane + 1) * N + p] = v.y;
+  S[(size_t)(plane + 2) * N + p] = v.z;
+}
+__device__ __forceinline__ m33 ldm33(const float *__restrict__ S, int N, int plane, int p) {
+  m33 m;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m.a[i / 3][i % 3] = __ldg(S + (size_t)(plane + i) * N + p);
+  return m;
+}
+__device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m33 &m) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
+}
+
+__device__ __forceinline__ int cell_index(const DexEnv &E, int x, int y, int z) {
+  int nby = E.gy >> 2, nbz = E.gz >> 2;
+  int blk = E.blk_off + ((x >> 2) * nby + (y >> 2)) * nbz + (z >> 2);
+  return (blk << 6) + ((x & 3) << 4) + ((y & 3) << 2) + (z & 3);
+}
+
+__device__ __forceinline__ bool stencil_in_grid(const DexEnv &E, const Stencil &st) {
+  return st.base[0] >= 0 && st.base[1] >= 0 && st.base[2] >= 0 && st.base[0] + 2 < E.gx &&
+         st.base[1] + 2 < E.gy && st.base[2] + 2 < E.gz;
+}
+
+// 32-wide bitonic sort of (key, idx) across the warp, ascending by (key, idx).
+__device__ __forceinline__ void warp_sort(int &key, int &idx, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      int ok = __shfl_xor_sync(kFull, key, j);
+      int oi = __shfl_xor_sync(kFull, idx, j);
+      bool up = (lane & k) == 0;
+      bool lower = (lane & j) == 0;
+      bool other_less = ok < key || (ok == key && oi < idx);
+      if ((lower == up) ? other_less : !other_less) {
+        key = ok;
+        idx = oi;
+      }
+    }
+  }
+}
+
+// Suffix sum within contiguous segments; the segment head ends with the total.
+__device__ __forceinline__ float seg_sum(float v, int lane, int seg_end) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    float t = __shfl_down_sync(kFull, v, off);
+    if (lane + off <= seg_end) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, float d) {
+  atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+  return v;
+}
+
+__device__ __forceinline__ void mark_block(const DexBatch &B, int X, int blk) {
+  uint32_t *flag = B.block_flag[X] + blk;
+  if (*reinterpret_cast<volatile uint32_t *>(flag) == 0u) {
+    if (atomicExch(flag, 1u) == 0u) {
+      int slot = atomicAdd(B.block_count + X, 1);
+      B.block_list[X][slot] = blk;
+    }
+  }
+}
+
+__device__ __forceinline__ void load_pose(const float *__restrict__ P, int b, BodyPose &o) {
+  float4 a = __ldg(reinterpret_cast<const float4 *>(P) + 2 * b);
+  float4 q = __ldg(reinterpret_cast<const float4 *>(P) + 2 * b + 1);
+  o.p = mk3(a.x, a.y, a.z);
+  o.q = mkq(q.x, q.y, q.z, q.w);
+}
+__device__ __forceinline__ void load_shape(const float *__restrict__ S, int b, BodyShape &o) {
+  float4 a = __ldg(reinterpret_cast<const float4 *>(S) + 2 * b);
+  float4 q = __ldg(reinterpret_cast<const float4 *>(S) + 2 * b + 1);
+  o.tfsr = mkq(a.x, a.y, a.z, a.w);
+  o.args = mkq(q.x, q.y, q.z, q.w);
+}
+
+// Per-lane particle selection shared by the scatter kernels: lanes are sorted
+// by stencil base so that equal cells are contiguous.  Returns the particle
+// index (valid even when !live) and fills the segment info.
+struct Lane {
+  int p;
+  bool live, head, lone;
+  int seg_end;
+};
+
+__device__ __forceinline__ Lane sorted_lane(const DexBatch &B, const DexEnv &E, const float *__restrict__ S,
+                                            int first) {
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const int wfirst = first + (threadIdx.x & ~31);
+  int loc = first + threadIdx.x;
+  int key = INT_MAX;
+  if (loc < E.n) {
+    Stencil st;
+    make_stencil(ldf3(S, N, PX, E.p_off + loc), E.inv_dx, st);
+    if (stencil_in_grid(E, st)) {
+      key = (st.base[0] * E.gy + st.base[1]) * E.gz + st.base[2];
+    } else {
+      atomicOr(B.error, DEXMPM_ERR_OUT_OF_GRID);
+    }
+  }
+  int src = lane;
+  warp_sort(key, src, lane);
+  Lane L;
+  L.live = key != INT_MAX;
+  L.p = E.p_off + (L.live ? wfirst + src : 0);
+  const unsigned same = __match_any_sync(kFull, key);
+  L.seg_end = 31 - __clz(same);
+  L.head = L.live && lane == __ffs(same) - 1;
+  L.lone = __all_sync(kFull, __popc(same) == 1);
+  return L;
+}
+
+// =================================================================== P2G
+// integrator.cu:84-100 (compute_svd) fused with :312-394 (p2g).
+__global__ void __launch_bounds__(256) k_p2g(DexBatch B, int X, const float *__restrict__ S,
+                                             float *__restrict__ Snext) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const Lane L = sorted_lane(B, E, S, first);
+  const int p = L.p;
+
+  const f3 x = ldf3(S, N, PX, p);
+  const f3 v = ldf3(S, N, PV, p);
+  const m33 F = ldm33(S, N, PF, p);
+  const m33 C = ldm33(S, N, PC, p);
+  const float m = L.live ? __ldg(B.mass + p) : 0.f;
+  const float vol = __ldg(B.vol + p);
+  const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
+              ys = __ldg(B.mu_lam_yield + 2 * N + p);
+
+  const m33 Et = deviation_tmp(F, C, E.dt);
+  const SVD3 sv = svd3_from_deviation(Et);
+  m33 Ft = Et;
+  Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
+  const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
+  if (Snext != nullptr && L.live) stm33(Snext, N, PF, p, pl.newF);
+
+  const float scale = L.live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
+  const m33 A = pl.P * scale + C * m;
+  const f3 mom = v * m;
+
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  float *grid = B.grid[X];
+
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+        const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
+                            ((float)k - st.fx[2]) * E.dx);
+        f3 c = (mom + mv(A, dpos)) * w;
+        float cm = m * w;
+        if (!L.lone) {
+          c.x = seg_sum(c.x, lane, L.seg_end);
+          c.y = seg_sum(c.y, lane, L.seg_end);
+          c.z = seg_sum(c.z, lane, L.seg_end);
+          cm = seg_sum(cm, lane, L.seg_end);
+        }
+        if (L.head) {
+          int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+          red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, cm);
+        }
+      }
+
+  if (L.head) {
+    const int nby = E.gy >> 2, nbz = E.gz >> 2;
+    const int b0x = st.base[0] >> 2, b1x = (st.base[0] + 2) >> 2;
+    const int b0y = st.base[1] >> 2, b1y = (st.base[1] + 2) >> 2;
+    const int b0z = st.base[2] >> 2, b1z = (st.base[2] + 2) >> 2;
+    for (int bx = b0x; bx <= b1x; ++bx)
+      for (int by = b0y; by <= b1y; ++by)
+        for (int bz = b0z; bz <= b1z; ++bz) mark_block(B, X, E.blk_off + (bx * nby + by) * nbz + bz);
+  }
+}
+
+// ============================================================ grid update
+// integrator.cu:647-777 on the active blocks of epoch X, then clearing of the
+// blocks of the previous epoch (Y).  The last CTA to finish resets the list
+// count of Y (ticket on done_counter; no CTA waits on another).
+__global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, const float *__restrict__ pose,
+                                                 const float *__restrict__ next_pose, int clear_grads) {
+  const int Y = X ^ 1;
+  const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  const int per_cta = blockDim.x >> 6;
+  const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
+  const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(B.grid[X]);
+  float4 *vout = reinterpret_cast<float4 *>(B.vout);
+  for (int item = blockIdx.x * per_cta + sub; item < cnt; item += gridDim.x * per_cta) {
+    const int blk = B.block_list[X][item];
+    const DexEnv E = B.envs[B.block_env[blk]];
+    const int local = blk - E.blk_off;
+    const int nby = E.gy >> 2, nbz = E.gz >> 2;
+    const int bx = local / (nby * nbz), by = (local / nbz) % nby, bz = local % nbz;
+    const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
+    const int ci = (blk << 6) + cell;
+    const float4 g = grid[ci];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g.w > kMassEps) {
+      const float inv_m = 1.f / g.w;
+      f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
+      const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
+      for (int b = 0; b < E.n_bodies; ++b) {
+        BodyPose cur, nxt;
+        BodyShape sh;
+        load_pose(pose, E.body_off + b, cur);
+        load_pose(next_pose, E.body_off + b, nxt);
+        load_shape(B.body_shape, E.body_off + b, sh);
+        contact_forward(gx, v, cur, nxt, sh, E.dt);
+      }
+      v = boundary_forward(v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
+      out = make_float4(v.x, v.y, v.z, g.w);
+    }
+    vout[ci] = out;
+  }
+  // clear the previous epoch's blocks
+  const int cnt_y = *reinterpret_cast<volatile int *>(B.block_count + Y);
+  float4 *gy = reinterpret_cast<float4 *>(B.grid[Y]);
+  float4 *vgy = reinterpret_cast<float4 *>(B.vout_grad[Y]);
+  float4 *igy = reinterpret_cast<float4 *>(B.in_grad[Y]);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int item = blockIdx.x * per_cta + sub; item < cnt_y; item += gridDim.x * per_cta) {
+    const int blk = B.block_list[Y][item];
+    const int ci = (blk << 6) + cell;
+    gy[ci] = z4;
+    if (clear_grads) {
+      vgy[ci] = z4;
+      igy[ci] = z4;
+    }
+    if (cell == 0) B.block_flag[Y][blk] = 0u;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned ticket = atomicAdd(B.done_counter, 1u);
+    if (ticket == gridDim.x - 1) {
+      B.block_count[Y] = 0;
+      *B.done_counter = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// =================================================================== G2P
+// integrator.cu:1059-1109.
+__global__ void __launch_bounds__(256) k_g2p(DexBatch B, const float *__restrict__ S, float *__restrict__ Snext) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int loc = first + threadIdx.x;
+  if (loc >= E.n) return;
+  const int N = B.n_particles;
+  const int p = E.p_off + loc;
+  const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  if (!stencil_in_grid(E, st)) return;  // reported by P2G
+  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(B.vout);
+  f3 nv = mk3(0.f, 0.f, 0.f);
+  m33 nC = mzero();
+  const float c4 = 4.f * E.inv_dx;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+        const float4 g = __ldg(vout + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k));
+        const f3 gv = mk3(g.x, g.y, g.z);
+        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
+        nv += gv * w;
+        nC += outer(gv, dpos) * (w * c4);
+      }
+  f3 nx = x + nv * E.dt;
+  const float lo = E.ground_height * E.dx;
+  nx.x = fmaxf(fminf(nx.x, (E.gx - 3.f) * E.dx), lo);
+  nx.y = fmaxf(fminf(nx.y, (E.gy - 3.f) * E.dx), lo);
+  nx.z = fmaxf(fminf(nx.z, (E.gz - 3.f) * E.dx), lo);
+  stf3(Snext, N, PX, p, nx);
+  stf3(Snext, N, PV, p, nv);
+  stm33(Snext, N, PC, p, nC);
+}
+
+// ============================================================ G2P adjoint
+// integrator.cu:1527-1614.  Writes (not adds) the x gradient of state s.
+__global__ void __launch_bounds__(256) k_g2p_grad(DexBatch B, int X, const float *__restrict__ S,
+                                                  const float *__restrict__ Snext, const float *__restrict__ Gnext,
+                                                  float *__restrict__ G) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const Lane L = sorted_lane(B, E, S, first);
+  const int p = L.p;
+  const f3 x = ldf3(S, N, PX, p);
+  f3 gx = ldf3(Gnext, N, PX, p);
+  f3 gnv = ldf3(Gnext, N, PV, p);
+  const m33 gC = L.live ? ldm33(Gnext, N, PC, p) : mzero();
+  const f3 nx = x + ldf3(Snext, N, PV, p) * E.dt;
+  const float lo = E.ground_height * E.dx;
+  if (nx.x > (E.gx - 3.f) * E.dx || nx.x < lo) gx.x = 0.f;
+  if (nx.y > (E.gy - 3.f) * E.dx || nx.y < lo) gx.y = 0.f;
+  if (nx.z > (E.gz - 3.f) * E.dx || nx.z < lo) gx.z = 0.f;
+  gnv += gx * E.dt;
+  if (!L.live) gnv = mk3(0.f, 0.f, 0.f);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  float w1[3][3];
+  make_dweights(st, E.inv_dx, w1);
+  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(B.vout);
+  float *vg = B.vout_grad[X];
+  const float c4 = 4.f * E.inv_dx;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
+        const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+        const float4 g4 = L.live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const f3 gv = mk3(g4.x, g4.y, g4.z);
+        const float xx = w * c4;
+        f3 ggv = gnv * w + mv(gC, dpos) * xx;
+        if (!L.lone) {
+          ggv.x = seg_sum(ggv.x, lane, L.seg_end);
+          ggv.y = seg_sum(ggv.y, lane, L.seg_end);
+          ggv.z = seg_sum(ggv.z, lane, L.seg_end);
+        }
+        if (L.head) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
+        gx += mtv(gC, gv) * (-E.inv_dx * xx);
+        const float gw = dot(gnv, gv) + c4 * dot(gv, mv(gC, dpos));
+        const f3 dw = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
+                          st.w[0][i] * st.w[1][j] * w1[2][k]);
+        gx += dw * gw;
+      }
+  if (L.live) stf3(G, N, PX, p, gx);
+}
+
+// ===================================================== grid update adjoint
+// integrator.cu:779-1057.  The per-body velocities entering each contact are
+// replayed here from (m, mv) instead of being stored by the forward.  Body-pose
+// gradients are reduced in the warp before one atomic per warp and value.
+__global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
+                                                      const float *__restrict__ next_pose, float *__restrict__ bgrad,
+                                                      float *__restrict__ next_bgrad) {
+  const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  const int per_cta = blockDim.x >> 6;
+  const int lane = threadIdx.x & 31;
+  const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
+  const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(B.grid[X]);
+  const float4 *__restrict__ vgrad = reinterpret_cast<const float4 *>(B.vout_grad[X]);
+  float4 *igrad = reinterpret_cast<float4 *>(B.in_grad[X]);
+  // uniform trip count per CTA so that whole warps run the body loop together
+  const int stride = gridDim.x * per_cta;
+  const int trips = (cnt + stride - 1) / stride;
+  for (int t = 0; t < trips; ++t) {
+    const int item = t * stride + blockIdx.x * per_cta + sub;
+    const bool in_list = item < cnt;
+    const int blk = in_list ? B.block_list[X][item] : 0;
+    const DexEnv E = B.envs[B.block_env[blk]];
+    const int local = blk - E.blk_off;
+    const int nby = E.gy >> 2, nbz = E.gz >> 2;
+    const int bx = local / (nby * nbz), by = (local / nbz) % nby, bz = local % nbz;
+    const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
+    const int ci = (blk << 6) + cell;
+    const float4 g = grid[ci];
+    const bool active = in_list && g.w > kMassEps;
+    const float inv_m = active ? 1.f / g.w : 0.f;
+    const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
+    // forward replay
+    f3 vin[DEXMPM_MAX_BODIES];
+    uint32_t touched = 0u;
+    f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
+    const int nbod = in_list ? E.n_bodies : 0;
+    if (active) {
+      for (int b = 0; b < nbod; ++b) {
+        BodyPose cur, nxt;
+        BodyShape sh;
+        load_pose(pose, E.body_off + b, cur);
+        load_pose(next_pose, E.body_off + b, nxt);
+        load_shape(B.body_shape, E.body_off + b, sh);
+        f3 before = v;
+        if (contact_forward(gx, v, cur, nxt, sh, E.dt)) {
+          vin[b] = before;
+          touched |= 1u << b;
+        }
+      }
+    }
+    const float4 gv4 = active ? vgrad[ci] : make_float4(0.f, 0.f, 0.f, 0.f);
+    f3 gv = boundary_backward(mk3(gv4.x, gv4.y, gv4.z), v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
+    // the warp's lanes share one block, hence one env and one body count
+    for (int b = nbod - 1; b >= 0; --b) {
+      const bool hit = (touched >> b) & 1u;
+      if (!__any_sync(kFull, hit)) continue;
+      float gc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float gn[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (hit) {
+        BodyPose cur, nxt;
+        BodyShape sh;
+        load_pose(pose, E.body_off + b, cur);
+        load_pose(next_pose, E.body_off + b, nxt);
+        load_shape(B.body_shape, E.body_off + b, sh);
+        contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn);
+      }
+#pragma unroll
+      for (int c = 0; c < 7; ++c) {
+        float a = warp_sum(gc[c]);
+        float n = warp_sum(gn[c]);
+        if (lane == 0) {
+          const int o = 8 * (E.body_off + b) + (c < 3 ? c : c + 1);
+          atomicAdd(bgrad + o, a);
+          atomicAdd(next_bgrad + o, n);
+        }
+      }
+    }
+    if (active) {
+      const f3 mom = mk3(g.x, g.y, g.z);
+      igrad[ci] = make_float4(gv.x * inv_m, gv.y * inv_m, gv.z * inv_m, -inv_m * inv_m * dot(mom, gv));
+    }
+  }
+}
+
+// ============================================================ P2G adjoint
+// integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad).
+// Adds to the x gradient written by k_g2p_grad and writes v, F, C gradients.
+__global__ void __launch_bounds__(128) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
+                                                  const float *__restrict__ Gnext, float *__restrict__ G,
+                                                  int split) {
+  const int tile = blockIdx.x / split, part = blockIdx.x % split;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int loc = first + part * blockDim.x + threadIdx.x;
+  if (loc >= E.n) return;
+  const int N = B.n_particles;
+  const int p = E.p_off + loc;
+  const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  if (!stencil_in_grid(E, st)) return;
+  const f3 v = ldf3(S, N, PV, p);
+  const m33 F = ldm33(S, N, PF, p);
+  const m33 C = ldm33(S, N, PC, p);
+  const float m = __ldg(B.mass + p), vol = __ldg(B.vol + p);
+  const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
+              ys = __ldg(B.mu_lam_yield + 2 * N + p);
+  const m33 Et = deviation_tmp(F, C, E.dt);
+  const SVD3 sv = svd3_from_deviation(Et);
+  m33 Ft = Et;
+  Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
+  const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
+  const float gss = -E.dt * E.inv_dx * vol * 4.f * E.inv_dx;
+  const m33 A = pl.P * gss + C * m;
+
+  float w1[3][3];
+  make_dweights(st, E.inv_dx, w1);
+  const float4 *__restrict__ ig = reinterpret_cast<const float4 *>(B.in_grad[X]);
+  m33 g_stress = mzero(), g_C = mzero();
+  f3 g_x = mk3(0.f, 0.f, 0.f), g_v = mk3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float Nw = st.w[0][i] * st.w[1][j] * st.w[2][k];
+        const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx, ((float)k - st.fx[2]) * E.dx);
+        const float4 g4 = __ldg(ig + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k));
+        const f3 gov = mk3(g4.x, g4.y, g4.z);
+        const f3 gN = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
+                          st.w[0][i] * st.w[1][j] * w1[2][k]);
+        const m33 tmp = outer(gov, dpos);
+        g_stress += tmp * (Nw * gss);
+        g_C += tmp * (Nw * m);
+        g_v += gov * (Nw * m);
+        g_x += gN * (g4.w * m + dot(v, gov) * m + dot(mv(A, dpos), gov));
+        g_x -= mtv(A, gov) * Nw;
+      }
+
+  // stress -> (U, V, sigma, F_tmp) gradients (integrator.cu:541-625)
+  const m33 &nF = pl.newF;
+  const m33 NmR = usv(sv.U, pl.dm1, sv.V);  // newF - U V^T without cancellation
+  const m33 g_r = mm(g_stress, nF) * (-2.f * mu);
+  m33 gU = mm(g_r, sv.V);
+  m33 gV = mm(mT(g_r), sv.U);
+  const m33 g_nF = ldm33(Gnext, N, PF, p) + (mm(mT(g_stress), NmR) + mm(g_stress, nF)) * (2.f * mu);
+  const float g_J = ((2.f * pl.J - 1.f) * lam) * trace(g_stress);
+  f3 g_s = mk3(0.f, 0.f, 0.f);
+  m33 g_Ft = mzero();
+  if (pl.yielded) {
+    const f3 ee = pl.expe;
+    const m33 ed = mdiag(ee);
+    gU += mm(mm(g_nF, sv.V), ed);
+    gV += mm(mm(mT(g_nF), sv.U), ed);
+    const m33 t = mm(mm(mT(sv.U), g_nF), sv.V);
+    const f3 Fpart = mk3(t.a[0][0], t.a[1][1], t.a[2][2]);
+    const f3 Jpart = mk3(g_J * ee.y * ee.z, g_J * ee.x * ee.z, g_J * ee.x * ee.y);
+    f3 g_e = hadamard(ee, Jpart + Fpart);
+    const f3 eh = pl.eps_hat;
+    const float ehn = pl.eps_hat_norm;
+    f3 g_eh = g_e * (-pl.delta_gamma / ehn);
+    const float g_ehn = -dot(eh * (1.f / ehn), g_e) * (ys / (2.f * mu)) / ehn;
+    g_eh += eh * (g_ehn / ehn);
+    const float sm = (g_eh.x + g_eh.y + g_eh.z) * (1.f / 3.f);
+    g_e += mk3(g_eh.x - sm, g_eh.y - sm, g_eh.z - sm);
+    if (sv.s.x >= kSigClip) g_s.x += g_e.x / sv.s.x;
+    if (sv.s.y >= kSigClip) g_s.y += g_e.y / sv.s.y;
+    if (sv.s.z >= kSigClip) g_s.z += g_e.z / sv.s.z;
+  } else {
+    g_s = mk3(g_J * sv.s.y * sv.s.z, g_J * sv.s.x * sv.s.z, g_J * sv.s.x * sv.s.y);
+    g_Ft = g_nF;
+  }
+  const m33 Gt = svd_backward(sv, gU, g_s, gV, g_Ft);
+  // F_tmp = (I + dt C) F
+  const m33 gC_total = g_C + mm(Gt, mT(F)) * E.dt;
+  m33 IdtC = C * E.dt;
+  IdtC.a[0][0] += 1.f; IdtC.a[1][1] += 1.f; IdtC.a[2][2] += 1.f;
+  const m33 gF = mm(mT(IdtC), Gt);
+  const f3 gx0 = mk3(G[p], G[(size_t)N + p], G[(size_t)2 * N + p]);
+  stf3(G, N, PX, p, gx0 + g_x);
+  stf3(G, N, PV, p, g_v);
+  stm33(G, N, PF, p, gF);
+  stm33(G, N, PC, p, gC_total);
+}
+
+__global__ void k_reset_counts(DexBatch B) {
+  if (threadIdx.x == 0) {
+    B.block_count[0] = 0;
+    B.block_count[1] = 0;
+    *B.done_counter = 0u;
+    *B.error = 0;
+  }
+}
+
+int check_launch() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
+
+bool valid(const DexBatch *b) {
+  return b && b->envs && b->tiles && b->block_env && b->mass && b->vol && b->mu_lam_yield && b->grid[0] &&
+         b->grid[1] && b->vout && b->block_flag[0] && b->block_flag[1] && b->block_list[0] && b->block_list[1] &&
+         b->block_count && b->done_counter && b->error && b->n_tiles >= 0 && b->n_blocks > 0 &&
+         (b->tile_size == 64 || b->tile_size == 128 || b->tile_size == 256) && b->grid_ctas > 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *dexmpm_version(void) { return "dexmpm 0.1 sm_103a"; }
+
+int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream) {
+  if (!valid(b)) return DEXMPM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t cells = (size_t)b->n_blocks * 64 * sizeof(float4);
+  for (int k = 0; k < 2; ++k) {
+    if (cudaMemsetAsync(b->grid[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+    if (b->vout_grad[k] && cudaMemsetAsync(b->vout_grad[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+    if (b->in_grad[k] && cudaMemsetAsync(b->in_grad[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+    if (cudaMemsetAsync(b->block_flag[k], 0, (size_t)b->n_blocks * sizeof(uint32_t), s) != cudaSuccess)
+      return DEXMPM_ERR_LAUNCH;
+  }
+  if (cudaMemsetAsync(b->vout, 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  k_reset_counts<<<1, 32, 0, s>>>(*b);
+  return check_launch();
+}
+
+int dexmpm_p2g(const DexBatch *b, int epoch, const float *S, float *Snext, dexmpm_stream_t stream) {
+  if (!valid(b) || !S) return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  k_p2g<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Snext);
+  return check_launch();
+}
+
+int dexmpm_grid_op(const DexBatch *b, int epoch, const float *pose, const float *next_pose, int clear_grads,
+                   dexmpm_stream_t stream) {
+  if (!valid(b) || (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape))) return DEXMPM_ERR_ARG;
+  if (clear_grads && (!b->vout_grad[0] || !b->vout_grad[1] || !b->in_grad[0] || !b->in_grad[1]))
+    return DEXMPM_ERR_ARG;
+  k_grid_op<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, epoch & 1, pose, next_pose, clear_grads);
+  return check_launch();
+}
+
+int dexmpm_g2p(const DexBatch *b, int epoch, const float *S, float *Snext, dexmpm_stream_t stream) {
+  (void)epoch;
+  if (!valid(b) || !S || !Snext) return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  k_g2p<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, S, Snext);
+  return check_launch();
+}
+
+int dexmpm_substep(const DexBatch *b, int epoch, const float *S, float *Snext, const float *pose,
+                   const float *next_pose, int clear_grads, dexmpm_stream_t stream) {
+  int rc = dexmpm_p2g(b, epoch, S, Snext, stream);
+  if (rc) return rc;
+  rc = dexmpm_grid_op(b, epoch, pose, next_pose, clear_grads, stream);
+  if (rc) return rc;
+  return dexmpm_g2p(b, epoch, S, Snext, stream);
+}
+
+int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *S, const float *Snext, const float *Gnext,
+                        float *G, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
+                        dexmpm_stream_t stream) {
+  if (!valid(b) || !S || !Snext || !Gnext || !G || !b->vout_grad[0] || !b->vout_grad[1] || !b->in_grad[0] ||
+      !b->in_grad[1])
+    return DEXMPM_ERR_ARG;
+  if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad)) return DEXMPM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int X = epoch & 1;
+  if (b->n_tiles > 0) k_g2p_grad<<<b->n_tiles, b->tile_size, 0, s>>>(*b, X, S, Snext, Gnext, G);
+  int rc = check_launch();
+  if (rc) return rc;
+  k_grid_op_grad<<<b->grid_ctas, 256, 0, s>>>(*b, X, pose, next_pose, bgrad, next_bgrad);
+  rc = check_launch();
+  if (rc) return rc;
+  if (b->n_tiles > 0) {
+    // the adjoint is register-heavy: 128-thread CTAs, ceil(tile/128) per tile
+    const int cta = b->tile_size < 128 ? b->tile_size : 128;
+    const int split = b->tile_size / cta;
+    k_p2g_grad<<<b->n_tiles * split, cta, 0, s>>>(*b, X, S, Gnext, G, split);
+  }
+  return check_launch();
+}
+
+int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {
+  if (!b || !b->error || !out) return DEXMPM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(out, b->error, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return DEXMPM_ERR_LAUNCH;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  if (cudaMemsetAsync(b->error, 0, sizeof(int32_t), s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  return DEXMPM_OK;
+}
+
+}  // extern "C"

@@ -116,6 +116,13 @@ DX_HD f3 qrot(qf q, f3 v) {
   f3 uv = cross(qv, v), uuv = cross(qv, uv);
   return v + 2.f * (q.w * uv + uuv);
 }
+// q*v - v: the rotation increment, without forming v + (small) and
+// subtracting v again
+DX_HD f3 qrot_delta(qf q, f3 v) {
+  f3 qv = mk3(q.x, q.y, q.z);
+  f3 uv = cross(qv, v), uuv = cross(qv, uv);
+  return 2.f * (q.w * uv + uuv);
+}
 DX_HD f3 xform(f3 p, qf q, f3 pt) { return p + qrot(q, pt); }            // quat.h:89-92
 DX_HD f3 xform_inv(f3 p, qf q, f3 pt) { return qrot(qinv(q), pt - p); }  // quat.h:94-97
 // adjoint of q*v (quat.h:25-49)
@@ -395,7 +402,8 @@ struct Plastic {
   bool yielded;
   f3 eps_hat;   // deviatoric log strain and its norm (for the adjoint)
   float eps_hat_norm, delta_gamma;
-  f3 expe;      // projected singular values when yielded
+  f3 expe;      // singular values of newF
+  f3 dm1;       // expe - 1 without cancellation
 };
 
 DX_HD Plastic constitutive(const SVD3 &sv, const m33 &Ftmp, float mu, float lam, float yield) {
@@ -416,6 +424,7 @@ DX_HD Plastic constitutive(const SVD3 &sv, const m33 &Ftmp, float mu, float lam,
     f3 ee = mk3(expf(ep[0]), expf(ep[1]), expf(ep[2]));
     f3 em1 = mk3(expm1f(ep[0]), expm1f(ep[1]), expm1f(ep[2]));
     o.expe = ee;
+    o.dm1 = em1;
     o.newF = usv(sv.U, ee, sv.V);
     o.J = ee.x * ee.y * ee.z;
     float Jm1 = expm1f(ep[0] + ep[1] + ep[2]);
@@ -425,6 +434,7 @@ DX_HD Plastic constitutive(const SVD3 &sv, const m33 &Ftmp, float mu, float lam,
     o.yielded = true;
   } else {
     o.expe = sv.s;
+    o.dm1 = sv.d;
     o.newF = Ftmp;
     o.J = sv.s.x * sv.s.y * sv.s.z;
     f3 d = sv.d;
@@ -447,6 +457,17 @@ struct BodyShape {
   qf args;
 };
 
+// Velocity of the body-frame point gxb = T_cur^-1(gx) carried by the body from
+// pose cur to pose nxt: (T_nxt(gxb) - gx) / dt (integrator.cu:716).  Written as
+//   (p1 - p0) + [Q1(u) - u] + [u - r],   r = gx - p0,  u = Q0^-1(r) = gxb,
+// which is the same quantity without subtracting two positions of size ~1
+// that differ by |v| dt (FP32 leaves ~3e-4 m/s of noise there at dt = 1e-4).
+DX_HD f3 body_velocity(f3 gx, f3 gxb, const BodyPose &cur, const BodyPose &nxt, float dt) {
+  f3 r = gx - cur.p;
+  f3 disp = (nxt.p - cur.p) + qrot_delta(nxt.q, gxb) + qrot_delta(qinv(cur.q), r);
+  return disp * (1.f / dt);
+}
+
 // One body contact on a grid node (integrator.cu:694-730).  Returns true when
 // the body touched the node.
 DX_HD bool contact_forward(f3 gx, f3 &v, const BodyPose &cur, const BodyPose &nxt, const BodyShape &sh, float dt) {
@@ -456,7 +477,7 @@ DX_HD bool contact_forward(f3 gx, f3 &v, const BodyPose &cur, const BodyPose &nx
   float infl = fminf(expf(-dist * softness), 1.f);
   if (!((softness > 0.f && infl > 0.1f) || dist <= 0.f)) return false;
   f3 nrm = qrot(cur.q, vnormalized(shape_grad(sh.tfsr, sh.args, gxb)));
-  f3 bv = (xform(nxt.p, nxt.q, gxb) - gx) * (1.f / dt);
+  f3 bv = body_velocity(gx, gxb, cur, nxt, dt);
   f3 rel = v - bv;
   float nc = dot(rel, nrm);
   f3 vt = rel - nrm * fminf(nc, 0.f);
@@ -544,7 +565,7 @@ DX_HD void contact_backward(f3 gx, f3 vo, f3 &gv, const BodyPose &cur, const Bod
   f3 un = shape_grad(sh.tfsr, sh.args, gxb);
   f3 rn = vnormalized(un);
   f3 nrm = qrot(cur.q, rn);
-  f3 bv = (xform(nxt.p, nxt.q, gxb) - gx) * (1.f / dt);
+  f3 bv = body_velocity(gx, gxb, cur, nxt, dt);
   f3 rel = vo - bv;
   float nc = dot(rel, nrm);
   f3 vtin = rel - nrm * fminf(nc, 0.f);

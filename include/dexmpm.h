@@ -1,0 +1,209 @@
+/* dexmpm.h -- C ABI of libdexmpm.so, the GB300 (sm_103a) MLS-MPM substep of
+ * DexDeform and its adjoint.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in replacements for the reference's extern "C" kernel launchers
+ *     (mpm/csrc/integrator.cu:1616-1985, bound by ctypes in mpm/types.py:130-290).
+ *     Same names, argument order, AoS layouts (vec3 = 3 floats, mat3 = 9 floats
+ *     row-major, quat = w,x,y,z) and dense x-major grids ((x*Gy + y)*Gz + z),
+ *     same accumulate-into-gradient contract.  `ivec3 const &` arguments are
+ *     passed as `const int *` (a C++ reference is a pointer at the ABI level).
+ *     Differences: each returns an int status (0 = success) instead of void,
+ *     and particles whose stencil leaves the grid are skipped and reported
+ *     (DEXMPM_ERR_OUT_OF_GRID through dexmpm_get_error) instead of writing out
+ *     of bounds.
+ *
+ *  2. The batched path (dexmpm_*): many environments of uneven particle counts
+ *     advanced by one launch per phase, particles in SoA planes, grids in 4^3
+ *     blocks with an active-block list.  Described by DexBatch below.
+ *
+ * All pointers are device pointers unless stated otherwise; `stream` is a
+ * cudaStream_t (0 = legacy default stream).  Nothing here allocates device
+ * memory: the caller owns every buffer.
+ */
+#ifndef DEXMPM_H
+#define DEXMPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *dexmpm_stream_t; /* cudaStream_t */
+
+enum {
+  DEXMPM_OK = 0,
+  DEXMPM_ERR_ARG = 1,          /* bad argument (null pointer, bad size, bad layout) */
+  DEXMPM_ERR_LAUNCH = 2,       /* CUDA launch error (cudaGetLastError after the launch) */
+  DEXMPM_ERR_OUT_OF_GRID = 4,  /* device flag: a particle stencil left the grid; it was skipped */
+  DEXMPM_ERR_TOO_MANY_BODIES = 8 /* more bodies per env than DEXMPM_MAX_BODIES */
+};
+
+#define DEXMPM_MAX_BODIES 32
+#define DEXMPM_BLOCK 4 /* grid block edge, cells */
+
+/* ===================================================================== 1 ==
+ * Reference-compatible launchers.  Each cites the reference launcher it
+ * replaces.  grid_lower must hold (0,0,0) (the reference never sets anything
+ * else: mpm/simulator.py:16,386); it is read on the device as in the reference.
+ */
+
+/* integrator.cu:1627-1638 -- F_tmp = (I + dt C) F and its SVD. */
+int compute_svd(float *F, float *C, float *newF, float *U, float *V, float *sig, float dt, int dim,
+                dexmpm_stream_t stream);
+
+/* integrator.cu:1640-1657 -- adjoint of compute_svd; accumulates F_grad, C_grad,
+ * overwrites newF_grad with the full F_tmp gradient. */
+int compute_svd_grad(float *F, float *C, float *U, float *V, float *sig, float *newF_grad, float *U_grad,
+                     float *V_grad, float *sig_grad, float *F_grad, float *C_grad, float dt, int dim,
+                     dexmpm_stream_t stream);
+
+/* integrator.cu:1659-1690 -- von Mises projection and APIC/stress scatter. */
+int p2g(float *particle_x, float *particle_v, float *particle_m, float *particle_vol, float *particle_F,
+        float *particle_U, float *particle_sig, float *particle_V, float *particle_C,
+        float *particle_mu_lam_yield, int *grid_lower, const int *grid_dim, float dx, float inv_dx, float dt,
+        float *out_particle_F, float *out_grid_mv, float *out_grid_m, int dim, dexmpm_stream_t stream);
+
+/* integrator.cu:1692-1742 -- adjoint of p2g. */
+int p2g_grad(float *particle_x, float *particle_v, float *particle_m, float *particle_vol, float *particle_F,
+             float *particle_U, float *particle_sig, float *particle_V, float *particle_C,
+             float *particle_mu_lam_yield, int *grid_lower, const int *grid_dim, float dx, float inv_dx,
+             float dt, float *out_particle_F, float *out_grid_mv, float *out_grid_m, float *particle_x_grad,
+             float *particle_v_grad, float *particle_F_grad, float *particle_C_grad, float *particle_U_grad,
+             float *particle_sig_grad, float *particle_V_grad, float *out_particle_F_grad,
+             float *out_grid_v_grad, float *out_grid_m_grad, int dim, dexmpm_stream_t stream);
+
+/* integrator.cu:1754-1779 -- gravity, sequential body contacts, walls and ground. */
+int grid_op_v2(float *grid_m, float *grid_v_in, float *grid_body_v_in, int *grid_lower, float *gravity,
+               float *body_pos, float *body_rot, float *next_body_pos, float *next_body_rot,
+               float *body_type_friction_softness_round, float *body_args, float dx, float inv_dx, float dt,
+               float ground_friction, float *out_grid_v, const int *grid_dim, int n_bodies,
+               dexmpm_stream_t stream);
+
+/* integrator.cu:1781-1819 -- adjoint of grid_op_v2. */
+int grid_op_v2_grad(float *grid_m, float *grid_v_in, float *grid_body_v_in, int *grid_lower, float *gravity,
+                    float *body_pos, float *body_rot, float *next_body_pos, float *next_body_rot,
+                    float *body_type_friction_softness_round, float *body_args, float *grid_m_grad,
+                    float *grid_v_in_grad, float *body_pos_grad, float *body_rot_grad, float *next_body_pos_grad,
+                    float *next_body_rot_grad, float dx, float inv_dx, float dt, float ground_friction,
+                    float *out_grid_v, float *out_grid_v_grad, const int *grid_dim, int n_bodies,
+                    dexmpm_stream_t stream);
+
+/* integrator.cu:1821-1835 -- APIC gather, advection and clamp. */
+int g2p(float *particle_x, float *grid_v, int *grid_lower, float dx, float inv_dx, float dt,
+        const int *grid_dim, float *out_particle_v, float ground_height, float *out_particle_C,
+        float *out_particle_x, int dim, dexmpm_stream_t stream);
+
+/* integrator.cu:1837-1861 -- adjoint of g2p. */
+int g2p_grad(float *particle_x, float *grid_v, int *grid_lower, float dx, float inv_dx, float dt,
+             const int *grid_dim, float *out_particle_v, float ground_height, float *out_particle_C,
+             float *out_particle_x, int dim, float *particle_x_grad, float *grid_v_grad,
+             float *out_particle_v_grad, float *out_particle_C_grad, float *out_particle_x_grad,
+             dexmpm_stream_t stream);
+
+/* integrator.cu:1935-1960 -- particle/body signed distances or their adjoint. */
+int compute_dist(float *particle_x, float *body_pos, float *body_rot, float *body_type_friction_softness_round,
+                 float *body_args, float *dist, int n_bodies, float *particle_x_grad, float *body_pos_grad,
+                 float *body_rot_grad, float *dist_grad, int compute_grad, int dim, dexmpm_stream_t stream);
+
+/* integrator.cu:1962-1984 -- per-object grid mass or its adjoint. */
+int particle2mass(float *particle_x, float *particle_m, int *grid_lower, const int *grid_dim, float dx,
+                  float inv_dx, float *out_grid_m, float *out_grid_m_grad, float *particle_x_grad,
+                  int *particle_ids, int id, int compute_grad, int dim, dexmpm_stream_t stream);
+
+/* Copy out and clear the error word shared by the launchers above (host
+ * pointer out; synchronous).  No counterpart in the reference, which has no
+ * error reporting (mpm/csrc/common.h:20-34). */
+int dexmpm_abi_get_error(int32_t *out);
+
+/* ===================================================================== 2 ==
+ * Batched path.
+ *
+ * Particle state slot: 24 float planes of n_particles each, plane-major:
+ *   x 0-2, v 3-5, F 6-14 (row-major), C 15-23.  Gradient slots use the same layout.
+ * Material: mass[n], vol[n], mu_lam_yield[3][n] (planes mu, lambda, yield).
+ * Grids: every env owns gx*gy*gz cells (dims multiples of 4) stored as 4^3
+ *   blocks; block b of the whole batch holds cells [64b, 64b+64), cell
+ *   (x,y,z) of env e is block blk_off + ((x>>2)*(gy/4) + (y>>2))*(gz/4) + (z>>2),
+ *   slot ((x&3)*16 + (y&3)*4 + (z&3)).  Cell values are float4:
+ *     grid[k]      (m v.x, m v.y, m v.z, m) after P2G
+ *     vout         (v.x, v.y, v.z, 0) after the grid update
+ *     vout_grad[k] dL/dv_out, in_grad[k] (dL/d(mv), dL/dm)
+ *   k = epoch & 1: each P2G starts an epoch; the grid update of epoch e
+ *   clears the blocks epoch e-1 used, so no per-substep memset is needed.
+ * Poses: [n_bodies][8] floats per substep boundary: p.x p.y p.z 0 q.w q.x q.y q.z.
+ * Body shapes: [n_bodies][8]: type friction softness round, args w x y z.
+ * Body-pose gradients: [n_bodies][8] in the pose layout, accumulated.
+ */
+typedef struct {
+  int32_t p_off, n, blk_off, body_off; /* first particle, count, first grid block, first body */
+  int32_t gx, gy, gz, n_bodies;        /* grid dims (multiples of 4), bodies */
+  float dx, inv_dx, dt, ground_friction;
+  float gravity[3];
+  float ground_height; /* cells; the particle clamp is [gh*dx, (G-3)*dx] */
+} DexEnv;              /* 64 bytes */
+
+typedef struct {
+  int32_t n_envs, n_particles, n_tiles, n_blocks;
+  int32_t n_bodies, tile_size, grid_ctas, reserved;
+  const DexEnv *envs;         /* [n_envs] */
+  const int32_t *tiles;       /* [n_tiles][2]: env, first particle within the env */
+  const int32_t *block_env;   /* [n_blocks]: owning env */
+  const float *mass;          /* [n_particles] */
+  const float *vol;           /* [n_particles] */
+  const float *mu_lam_yield;  /* [3][n_particles] */
+  float *grid[2];             /* [n_blocks*64] float4 */
+  float *vout;                /* [n_blocks*64] float4 */
+  float *vout_grad[2];        /* [n_blocks*64] float4 */
+  float *in_grad[2];          /* [n_blocks*64] float4 */
+  uint32_t *block_flag[2];    /* [n_blocks] */
+  int32_t *block_list[2];     /* [n_blocks] */
+  int32_t *block_count;       /* [2] */
+  uint32_t *done_counter;     /* [1] */
+  const float *body_shape;    /* [n_bodies][8] */
+  int32_t *error;             /* [1] sticky DEXMPM_ERR_* bits */
+} DexBatch;
+
+/* Zero every grid buffer, flag, list count and the error word.  Call once after
+ * allocation (and after any fault) -- the epochs keep them clean afterwards. */
+int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream);
+
+/* P2G of epoch `epoch`: SVD, von Mises, stress, APIC scatter of state slot s
+ * into grid[epoch&1]; appends the touched blocks to block_list[epoch&1].
+ * F_out (nullable) receives the projected F (9 planes at the F offset of the
+ * next state slot). */
+int dexmpm_p2g(const DexBatch *b, int epoch, const float *s, float *next_s, dexmpm_stream_t stream);
+
+/* Grid update of epoch `epoch` on its active blocks, with body poses at the
+ * substep start (pose) and end (next_pose); clears the blocks of epoch-1
+ * (their gradient buffers too when clear_grads != 0). */
+int dexmpm_grid_op(const DexBatch *b, int epoch, const float *pose, const float *next_pose, int clear_grads,
+                   dexmpm_stream_t stream);
+
+/* G2P of epoch `epoch`: x, v, C of next_s from s and vout. */
+int dexmpm_g2p(const DexBatch *b, int epoch, const float *s, float *next_s, dexmpm_stream_t stream);
+
+/* One forward substep: dexmpm_p2g + dexmpm_grid_op + dexmpm_g2p. */
+int dexmpm_substep(const DexBatch *b, int epoch, const float *s, float *next_s, const float *pose,
+                   const float *next_pose, int clear_grads, dexmpm_stream_t stream);
+
+/* Adjoint of one substep whose forward (p2g + grid_op) was just recomputed in
+ * epoch `epoch` from state slot s.  next_s is the state after the substep (its
+ * v sets the clamp mask), g_next the gradient of next_s, g the gradient of s
+ * (overwritten).  Body-pose gradients are added to bgrad / next_bgrad. */
+int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *s, const float *next_s, const float *g_next,
+                        float *g, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
+                        dexmpm_stream_t stream);
+
+/* Copy out and clear the device error word (host pointer out). */
+int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream);
+
+/* Library version string (host). */
+const char *dexmpm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -34,6 +34,13 @@ static inline int atomicMax(int *a, int b) { int o = *a; if (b > o) *a = b; retu
 static inline long long atomicMin(long long *a, long long b) { long long o = *a; if (b < o) *a = b; return o; }
 using std::max;
 using std::min;
+// CUDA's headers put float overloads of abs/log/exp in the global namespace
+// (vec3.h:111-119 calls ::abs, ::log, ::exp on floats); the host C library
+// only has int abs(int) and double log/exp there, and ::abs(float) would
+// truncate to an integer.  Give them the meaning they have under nvcc.
+static inline float abs(float a) { return fabsf(a); }
+static inline float log(float a) { return logf(a); }
+static inline float exp(float a) { return expf(a); }
 // CUDA's device headers overload min/max on mixed float/double arguments; the
 // host library does not, so give the mixed forms the device meaning.
 static inline double min(float a, double b) { return a < b ? (double)a : b; }

@@ -1,0 +1,66 @@
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
+
+
+def _ensure(path, script):
+    if not os.path.isfile(path):
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", script)], check=True, capture_output=True)
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle as O
+    _ensure(O.ORACLE_SO, "build_oracle.sh")
+    O.set_svd_mode("reference")
+    return O
+
+
+@pytest.fixture(scope="session")
+def native_lib():
+    from dexdeform_gb300 import _native as N
+    if not N.lib_available():
+        from dexdeform_gb300 import build as B
+        B.build()
+    return N.load()
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def golden_env(path):
+    """Rebuild the workloads.Env a fixture was generated from."""
+    from dexdeform_gb300 import workloads as W
+    z = np.load(path)
+    st = {k: z[f"s0_{k}"] if f"s0_{k}" in z else z[f"in_{k}"] for k in ("x", "v", "F", "C")}
+    env = W.Env(grid_dim=tuple(int(v) for v in z["grid_dim"]), dx=float(z["dx"]), dt=float(z["dt"]),
+                gravity=tuple(float(v) for v in z["gravity"]), ground_friction=float(z["ground_friction"]),
+                x=st["x"], v=st["v"], F=st["F"], C=st["C"], mass=z["mass"], vol=z["vol"],
+                mu_lam_yield=z["mu_lam_yield"], body_tfsr=z["body_tfsr"], body_args=z["body_args"],
+                poses=z["poses"])
+    return env, z
+
+
+def oracle_sim(O, env, backend="oracle"):
+    prm = O.SimParams(grid_dim=env.grid_dim, dx=env.dx, dt=env.dt, gravity=env.gravity,
+                      ground_friction=env.ground_friction)
+    return O.CpuMPM(backend, prm, O.Material(env.mass, env.vol, env.mu_lam_yield),
+                    O.Bodies(env.body_tfsr, env.body_args))
+
+
+gpu = pytest.mark.gpu

@@ -34,3 +34,73 @@ void host_constitutive(int n, const float *F, const float *C, float dt, const fl
   }
 }
 }
+
+// Serial host emulation of one forward substep with the product's FP32
+// arithmetic on a dense x-major grid (the schedule of mpm/simulator.py:561-571),
+// for CPU-side numerical checks against the FP64 oracle.  Body arrays:
+// pose [nb][8] (p xyz 0 q wxyz), shapes [nb][8] (tfsr, args).
+#include <vector>
+extern "C" void host_substep(int n, const float *x, const float *v, const float *F, const float *C, const float *mass,
+                             const float *vol, const float *mly, int gx, int gy, int gz, float dx, float dt,
+                             const float *gravity, float gf, int nb, const float *pose, const float *npose,
+                             const float *shapes, float *ox, float *ov, float *oF, float *oC) {
+  const float inv_dx = 1.f / dx;
+  std::vector<float> gm((size_t)gx * gy * gz, 0.f), gmv((size_t)gx * gy * gz * 3, 0.f), gv((size_t)gx * gy * gz * 3, 0.f);
+  auto idx = [&](int a, int b, int c) { return ((size_t)a * gy + b) * gz + c; };
+  for (int p = 0; p < n; ++p) {
+    m33 Fm = load9(F + 9 * p), Cm = load9(C + 9 * p);
+    m33 E = deviation_tmp(Fm, Cm, dt);
+    SVD3 s = svd3_from_deviation(E);
+    m33 Ft = E; Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
+    Plastic pl = constitutive(s, Ft, mly[3 * p], mly[3 * p + 1], mly[3 * p + 2]);
+    store9(oF + 9 * p, pl.newF);
+    m33 A = pl.P * (-dt * vol[p] * 4.f * inv_dx * inv_dx) + Cm * mass[p];
+    f3 mom = mk3(v[3 * p], v[3 * p + 1], v[3 * p + 2]) * mass[p];
+    Stencil st;
+    make_stencil(mk3(x[3 * p], x[3 * p + 1], x[3 * p + 2]), inv_dx, st);
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) for (int k = 0; k < 3; ++k) {
+      float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+      f3 dpos = mk3((i - st.fx[0]) * dx, (j - st.fx[1]) * dx, (k - st.fx[2]) * dx);
+      size_t id = idx(st.base[0] + i, st.base[1] + j, st.base[2] + k);
+      f3 c = (mom + mv(A, dpos)) * w;
+      gm[id] += mass[p] * w; gmv[3 * id] += c.x; gmv[3 * id + 1] += c.y; gmv[3 * id + 2] += c.z;
+    }
+  }
+  for (int a = 0; a < gx; ++a) for (int b = 0; b < gy; ++b) for (int c = 0; c < gz; ++c) {
+    size_t id = idx(a, b, c);
+    if (!(gm[id] > kMassEps)) continue;
+    float im = 1.f / gm[id];
+    f3 vv = mk3(gmv[3 * id] * im, gmv[3 * id + 1] * im, gmv[3 * id + 2] * im) + mk3(gravity[0], gravity[1], gravity[2]) * dt;
+    f3 gxw = mk3(a * dx, b * dx, c * dx);
+    for (int bb = 0; bb < nb; ++bb) {
+      BodyPose cur, nxt; BodyShape sh;
+      cur.p = mk3(pose[8 * bb], pose[8 * bb + 1], pose[8 * bb + 2]); cur.q = mkq(pose[8 * bb + 4], pose[8 * bb + 5], pose[8 * bb + 6], pose[8 * bb + 7]);
+      nxt.p = mk3(npose[8 * bb], npose[8 * bb + 1], npose[8 * bb + 2]); nxt.q = mkq(npose[8 * bb + 4], npose[8 * bb + 5], npose[8 * bb + 6], npose[8 * bb + 7]);
+      sh.tfsr = mkq(shapes[8 * bb], shapes[8 * bb + 1], shapes[8 * bb + 2], shapes[8 * bb + 3]);
+      sh.args = mkq(shapes[8 * bb + 4], shapes[8 * bb + 5], shapes[8 * bb + 6], shapes[8 * bb + 7]);
+      contact_forward(gxw, vv, cur, nxt, sh, dt);
+    }
+    vv = boundary_forward(vv, a, b, c, gx, gy, gz, gf);
+    gv[3 * id] = vv.x; gv[3 * id + 1] = vv.y; gv[3 * id + 2] = vv.z;
+  }
+  for (int p = 0; p < n; ++p) {
+    Stencil st;
+    f3 xp = mk3(x[3 * p], x[3 * p + 1], x[3 * p + 2]);
+    make_stencil(xp, inv_dx, st);
+    f3 nv = mk3(0.f, 0.f, 0.f); m33 nC = mzero();
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) for (int k = 0; k < 3; ++k) {
+      float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+      size_t id = idx(st.base[0] + i, st.base[1] + j, st.base[2] + k);
+      f3 g = mk3(gv[3 * id], gv[3 * id + 1], gv[3 * id + 2]);
+      nv += g * w;
+      nC += outer(g, mk3(i - st.fx[0], j - st.fx[1], k - st.fx[2])) * (w * 4.f * inv_dx);
+    }
+    f3 nx = xp + nv * dt;
+    nx.x = fmaxf(fminf(nx.x, (gx - 3.f) * dx), 3.f * dx);
+    nx.y = fmaxf(fminf(nx.y, (gy - 3.f) * dx), 3.f * dx);
+    nx.z = fmaxf(fminf(nx.z, (gz - 3.f) * dx), 3.f * dx);
+    ox[3 * p] = nx.x; ox[3 * p + 1] = nx.y; ox[3 * p + 2] = nx.z;
+    ov[3 * p] = nv.x; ov[3 * p + 1] = nv.y; ov[3 * p + 2] = nv.z;
+    store9(oC + 9 * p, nC);
+  }
+}
