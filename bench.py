@@ -1,0 +1,496 @@
+#!/usr/bin/env python
+"""Headline benchmark: batched differentiable MLS-MPM on one GB300.
+
+Workload (the batching configuration): 64 independent envs, each its own 64^3
+grid, particle counts log-uniform in [2,000, 30,000] (seeded), cube or
+ellipsoid objects, von Mises yield stress U[30, 80], 22 random-walk capsules
+per env; 10 env steps x 50 substeps, forward and forward+backward (adjoint with
+per-env-step checkpoints and substep recomputation), each env step replayed as
+a CUDA graph.  A step = one full rollout forward + loss + backward.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Metric: particle-substeps/s (forward+backward; forward-only and the plain
+per-env sequential path are reported beside it).  Under torchrun every rank
+runs its own replica batch (no collective on the data path; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-substeps/s fwd & fwd+bwd, batched vs plain, 1 GB300 @1e-3 tol; p50/p99"
+UNIT = "particle-substeps/s"
+N_ENVS, SUBSTEPS, ENV_STEPS = 64, 50, 10
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--envs", type=int, default=N_ENVS)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+def dist_setup(n_gpus):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        sm = sorted(r[0] for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[2]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows), "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------- workloads
+def build_batch(seed, n_envs):
+    from dexdeform_gb300 import workloads as W
+    return W.batch_envs(seed, n_envs=n_envs, steps=SUBSTEPS * ENV_STEPS)
+
+
+def targets_for(envs):
+    rng = np.random.default_rng(12345)
+    return [e.x + rng.normal(scale=0.01, size=e.x.shape).astype(np.float32) for e in envs]
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local):
+    import torch
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec, Rollout
+    from dexdeform_gb300 import _native as N
+
+    dev = torch.device("cuda", local)
+    envs = build_batch(rank, args.envs)
+    n_total = sum(e.n for e in envs)
+    work = n_total * SUBSTEPS * ENV_STEPS  # particle-substeps per rollout
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True)
+    R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS)
+    poses_h = E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs])
+    R.poses.copy_(torch.from_numpy(poses_h))
+    s0 = E.pack_state([e.state() for e in envs])
+    tgt = E.pack_state([{"x": t, "v": np.zeros_like(t), "F": np.zeros((len(t), 3, 3), np.float32),
+                         "C": np.zeros((len(t), 3, 3), np.float32)} for t in targets_for(envs)])
+    counts = torch.zeros(E.n_particles, device=dev)
+    for e, env in enumerate(envs):
+        counts[E.p_off[e]:E.p_off[e] + env.n] = 1.0 / env.n
+    g_final = torch.zeros_like(s0)
+
+    def loss_grad(final):
+        # L = sum_e mean_p |x - target|^2 ; dL/dx = 2 (x - target) / n_e
+        d = (final[0:3] - tgt[0:3]) * counts
+        g_final[0:3] = 2.0 * d
+        return (d * (final[0:3] - tgt[0:3])).sum()
+
+    def step():
+        final = R.forward(s0)
+        loss = loss_grad(final)
+        g0 = R.backward(g_final)
+        return loss, g0
+
+    def fwd_step():
+        return R.forward(s0)
+
+    # ----- warm-up (captures the graphs)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    launches0 = E.launches
+    # ----- timed fwd+bwd
+    per_step = []
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        ev[0].record()
+        for k in range(args.steps):
+            step()
+            ev[k + 1].record()
+        torch.cuda.synchronize()
+        barrier(world)
+    gpu_launches = E.launches - launches0
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    t_ms = ev[0].elapsed_time(ev[-1])
+    t_ms_max = max_over_ranks(t_ms, world)
+    work_all = sum_over_ranks(float(work), world)
+    value = work_all * args.steps / (t_ms_max / 1e3)
+    # ----- forward only
+    for _ in range(3):
+        fwd_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        fwd_step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    fwd_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    fwd_value = work_all * args.steps / (fwd_ms / 1e3)
+    # ----- end to end: inputs from pinned host, result back to host
+    s0_h = s0.cpu().pin_memory()
+    poses_pin = torch.from_numpy(poses_h).pin_memory()
+    g0_h = torch.empty_like(s0_h).pin_memory()
+    bg_h = torch.empty(R.bgrad.shape, dtype=torch.float32).pin_memory()
+    loss_h = torch.empty(1, dtype=torch.float32).pin_memory()
+    s0_dev = torch.empty_like(s0)
+
+    def e2e_step():
+        s0_dev.copy_(s0_h, non_blocking=True)
+        R.poses.copy_(poses_pin, non_blocking=True)
+        final = R.forward(s0_dev)
+        loss = loss_grad(final)
+        g0 = R.backward(g_final)
+        g0_h.copy_(g0, non_blocking=True)
+        bg_h.copy_(R.bgrad, non_blocking=True)
+        loss_h.copy_(loss.reshape(1), non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize()
+    host_ms = (time.perf_counter() - t0) * 1e3
+    barrier(world)
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), host_ms), world)
+    e2e_value = work_all * args.steps / (e2e_ms / 1e3)
+    h2d = s0_h.numel() * 4 + poses_pin.numel() * 4
+    d2h = g0_h.numel() * 4 + bg_h.numel() * 4 + 4
+
+    # ----- per-kernel timing (eager, CUDA events on the launching stream)
+    kt = kernel_times(E, R, s0, g_final)
+    roof = roofline(E, kt)
+    err = E.error_word()
+
+    plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
+    cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs, budget_s=12.0)
+
+    if rank == 0:
+        ps = sorted(per_step)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.batch_envs)",
+            "config": {"workload": "batch: 64 envs x 64^3 grid, log-uniform 2k-30k particles, 22 capsules/env, "
+                                   "10 env steps x 50 substeps, fwd+bwd with per-env-step checkpoints, CUDA graphs",
+                       "n_envs": len(envs), "particles_per_replica": n_total, "substeps": SUBSTEPS * ENV_STEPS,
+                       "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (per-step state traffic ~4 GB >> 129 MB L2)"},
+            "fwd": {"value": fwd_value, "unit": UNIT, "ms_per_step": fwd_ms / args.steps},
+            "latency_ms": {"p50": ps[len(ps) // 2], "p99": ps[min(len(ps) - 1, int(math.ceil(0.99 * len(ps))) - 1)],
+                           "what": "one fwd+bwd rollout of the whole batch"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(gpu_launches),
+            "roofline": roof,
+            "kernels_us": {k: round(v, 2) for k, v in kt.items()},
+            "error_word": err,
+        }
+        if plain is not None:
+            out["plain"] = plain
+            out["batched_vs_plain"] = {"fwd": fwd_value / plain["fwd"], "fwd_bwd": value / plain["fwd_bwd"]}
+        if cpu is not None:
+            out["cpu_baseline"] = cpu
+        out["clocks"] = clk.summary()
+        print(json.dumps(out))
+
+
+def kernel_times(E, R, s0, g_final):
+    """Average device time (us) of each kernel over one env step, from CUDA
+    events around eager launches on the current stream."""
+    import torch
+    from dexdeform_gb300 import _native as N
+    L, sp = E.lib, N.stream_ptr()
+    T = R.T
+    acc = {}
+
+    def timed(name, fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        acc.setdefault(name, []).append((a, b))
+
+    ring, ck = R.ring, R.ckpt
+    src = ck[0]
+    for s in range(T):
+        e, clear = E._next_epoch(False)
+        dst = ring[s + 1]
+        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, e, N.ptr(src), N.ptr(dst), sp), "p2g"))
+        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, e, N.ptr(R.poses[s]), N.ptr(R.poses[s + 1]), 1, sp),
+                                         "grid_op"))
+        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, e, N.ptr(src), N.ptr(dst), sp), "g2p"))
+        src = dst
+    gn, g = R.gbuf[1], R.gbuf[0]
+    gn.copy_(g_final)
+    for s in range(T - 1, -1, -1):
+        e, clear = E._next_epoch(True)
+        cur = ck[0] if s == 0 else ring[s]
+        nxt = ring[s + 1]
+        pz, pn = R.poses[s], R.poses[s + 1]
+        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, e, N.ptr(cur), None, sp), "p2g"))
+        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, e, N.ptr(pz), N.ptr(pn), 1, sp), "grid_op"))
+        timed("g2p_grad", lambda: N.check(L.dexmpm_g2p_grad(E._bp, e, N.ptr(cur), N.ptr(nxt), N.ptr(gn), N.ptr(g), sp),
+                                          "g2p_grad"))
+        timed("grid_op_grad", lambda: N.check(L.dexmpm_grid_op_grad(E._bp, e, N.ptr(pz), N.ptr(pn), N.ptr(R.bgrad[s]),
+                                                                    N.ptr(R.bgrad[s + 1]), sp), "grid_op_grad"))
+        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, e, N.ptr(cur), N.ptr(gn), N.ptr(g), sp), "p2g_grad"))
+        gn, g = g, gn
+    torch.cuda.synchronize()
+    return {k: 1e3 * sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in acc.items()}
+
+
+# Algorithmic bytes per particle (N) and per cell of the active blocks (A)
+# for each kernel: particle state read/written once, grid float4 cells once.
+ALG_BYTES = {
+    "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
+    "grid_op": (0, 48),        # (mv, m) read, v_out written, previous epoch's cells cleared
+    "g2p": (72, 16),           # x read, x v C written; v_out gathered
+    "g2p_grad": (96, 32),      # x, v', dL/d(x v C)' read, dL/dx written; v_out read, dL/dv_out scattered
+    "grid_op_grad": (0, 48),   # (mv, m), dL/dv_out read, dL/d(mv, m) written
+    "p2g_grad": (260, 16),     # x v F C + material + dL/dF', dL/dx read, dL/d(x v F C) written; dL/d(mv,m) gathered
+}
+
+
+def roofline(E, kt):
+    import torch
+    peak, src = peaks()
+    top = max(kt, key=kt.get)
+    n = sum(s.n for s in E.specs)
+    cells = int(E.block_count.sum().item()) * 32  # mean active blocks of the two live epochs x 64 cells / 2
+    bp, bc = ALG_BYTES[top]
+    alg = bp * n + bc * cells
+    achieved = alg / (kt[top] * 1e-6) / 1e9
+    return {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": src, "alg_bytes_per_launch": int(alg),
+            "avg_launch_us": kt[top], "traffic": None,
+            "note": "traffic from ncu: see profiles/ (capture on a reduced case, scaled per particle)"}
+
+
+def plain_rates(envs, dev, sample_every=8):
+    """Plain per-env sequential path: the reference's schedule (memsets + per-kernel
+    launches, full per-substep state storage) on the reference-compatible
+    launchers, one env at a time, for a sample of the batch's envs."""
+    import torch
+    from dexdeform_gb300.simulator import MPMSimulator
+    T = SUBSTEPS
+    fwd_t = bwd_t = 0.0
+    work = 0
+    for env in envs[::sample_every]:
+        sim = MPMSimulator(env.nb, n_particles=env.n, dx=env.dx, dt=env.dt, grid_size=(1, 1, 1), max_steps=T + 1,
+                           substeps=T, gravity=(0, -1, 0), ground_friction=env.ground_friction)
+        sim.init_particles(env.vol.astype(np.float64), env.mass.astype(np.float64), env.mu_lam_yield.astype(np.float64))
+        sim.init_bodies(env.body_tfsr[:, 0], env.body_tfsr[:, 2], env.body_tfsr[:, 1], env.body_tfsr[:, 3],
+                        env.body_args, None)
+        st = env.state()
+        pose0 = env.poses[0]
+        sim.set_state(0, (st["x"], st["v"], st["F"], st["C"], *[p for p in pose0]))
+        poses = torch.tensor(env.poses[:T + 1], device=dev)
+        for rep in range(2):
+            torch.cuda.synchronize()
+            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record()
+            for f in range(T):
+                sim.set_pose(sim.states[f + 1], poses[f + 1, :, :3], poses[f + 1, :, 3:])
+                sim.substep(f, clear_grad=True)
+            b.record()
+            sim.states[T].x_grad.t.normal_()
+            for f in range(T - 1, -1, -1):
+                sim.substep_grad(f)
+            c.record()
+            torch.cuda.synchronize()
+        fwd_t += a.elapsed_time(b) / 1e3
+        bwd_t += a.elapsed_time(c) / 1e3
+        work += env.n * T
+        del sim
+    return {"fwd": work / fwd_t, "fwd_bwd": work / bwd_t, "unit": UNIT,
+            "what": f"reference schedule on the reference-compatible launchers, one env at a time, "
+                    f"{len(envs[::sample_every])} sampled envs x 1 env step"}
+
+
+def cpu_baseline(envs, budget_s=12.0):
+    """FP64 C restatement (oracle/) on the host cores, the reference's schedule
+    (forward storing every substep state, then the adjoint), bounded sample."""
+    from oracle import oracle as O
+    O.set_svd_mode("reference")
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    work, done = 0, 0
+    T = 5
+    for env in envs:
+        prm = O.SimParams(grid_dim=env.grid_dim, dx=env.dx, dt=env.dt, gravity=env.gravity,
+                          ground_friction=env.ground_friction)
+        o = O.CpuMPM("oracle", prm, O.Material(env.mass, env.vol, env.mu_lam_yield),
+                     O.Bodies(env.body_tfsr, env.body_args))
+        states = [env.state()]
+        for t in range(T):
+            states.append(o.substep(states[-1], env.pose(t), env.pose(t + 1)))
+        g = {k: np.zeros_like(v, dtype=np.float64) for k, v in states[-1].items()}
+        g["x"] = np.ones_like(g["x"])
+        for t in range(T - 1, -1, -1):
+            g, _, _ = o.substep_grad(states[t], env.pose(t), env.pose(t + 1), states[t + 1]["v"], g)
+        work += env.n * T
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": work / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{done} envs of the batch x {T} substeps fwd+bwd (reference schedule), FP64, OpenMP",
+            "seconds": round(dt, 2)}
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    envs = build_batch(0, args.envs)
+    times = []
+    cpu = None
+    for k in range(args.warmup + args.steps):
+        c = cpu_baseline(envs, budget_s=6.0)
+        if k >= args.warmup:
+            times.append(c)
+        cpu = c
+    value = float(np.mean([c["value"] for c in times])) if times else cpu["value"]
+    n_total = sum(e.n for e in envs)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": n_total * SUBSTEPS * ENV_STEPS / value * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded, workloads.batch_envs)", "impl": "reference",
+           "config": {"workload": "batch: 64 envs x 64^3 grid, log-uniform 2k-30k particles, 22 capsules/env, "
+                                  "10 env steps x 50 substeps, fwd+bwd",
+                      "note": "the reference path is CUDA-only; its CPU stand-in is the FP64 C restatement "
+                              "(oracle/), timed on a bounded sample of the same envs each step"},
+           "cpu_baseline": {**cpu, "value": value},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        run_reference(args, rank, world)
+        return
+    rank, world, local = dist_setup(args.gpus)
+    run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

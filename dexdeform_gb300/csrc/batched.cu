@@ -654,28 +654,45 @@ int dexmpm_substep(const DexBatch *b, int epoch, const float *S, float *Snext, c
   return dexmpm_g2p(b, epoch, S, Snext, stream);
 }
 
+static bool grad_ok(const DexBatch *b) {
+  return valid(b) && b->vout_grad[0] && b->vout_grad[1] && b->in_grad[0] && b->in_grad[1];
+}
+
+int dexmpm_g2p_grad(const DexBatch *b, int epoch, const float *S, const float *Snext, const float *Gnext, float *G,
+                    dexmpm_stream_t stream) {
+  if (!grad_ok(b) || !S || !Snext || !Gnext || !G) return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  k_g2p_grad<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Snext, Gnext, G);
+  return check_launch();
+}
+
+int dexmpm_grid_op_grad(const DexBatch *b, int epoch, const float *pose, const float *next_pose, float *bgrad,
+                        float *next_bgrad, dexmpm_stream_t stream) {
+  if (!grad_ok(b)) return DEXMPM_ERR_ARG;
+  if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape)) return DEXMPM_ERR_ARG;
+  k_grid_op_grad<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, epoch & 1, pose, next_pose, bgrad, next_bgrad);
+  return check_launch();
+}
+
+int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *S, const float *Gnext, float *G,
+                    dexmpm_stream_t stream) {
+  if (!grad_ok(b) || !S || !Gnext || !G) return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  // the adjoint is register-heavy: 128-thread CTAs, tile_size/128 of them per tile
+  const int cta = b->tile_size < 128 ? b->tile_size : 128;
+  const int split = b->tile_size / cta;
+  k_p2g_grad<<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Gnext, G, split);
+  return check_launch();
+}
+
 int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *S, const float *Snext, const float *Gnext,
                         float *G, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
                         dexmpm_stream_t stream) {
-  if (!valid(b) || !S || !Snext || !Gnext || !G || !b->vout_grad[0] || !b->vout_grad[1] || !b->in_grad[0] ||
-      !b->in_grad[1])
-    return DEXMPM_ERR_ARG;
-  if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad)) return DEXMPM_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int X = epoch & 1;
-  if (b->n_tiles > 0) k_g2p_grad<<<b->n_tiles, b->tile_size, 0, s>>>(*b, X, S, Snext, Gnext, G);
-  int rc = check_launch();
+  int rc = dexmpm_g2p_grad(b, epoch, S, Snext, Gnext, G, stream);
   if (rc) return rc;
-  k_grid_op_grad<<<b->grid_ctas, 256, 0, s>>>(*b, X, pose, next_pose, bgrad, next_bgrad);
-  rc = check_launch();
+  rc = dexmpm_grid_op_grad(b, epoch, pose, next_pose, bgrad, next_bgrad, stream);
   if (rc) return rc;
-  if (b->n_tiles > 0) {
-    // the adjoint is register-heavy: 128-thread CTAs, ceil(tile/128) per tile
-    const int cta = b->tile_size < 128 ? b->tile_size : 128;
-    const int split = b->tile_size / cta;
-    k_p2g_grad<<<b->n_tiles * split, cta, 0, s>>>(*b, X, S, Gnext, G, split);
-  }
-  return check_launch();
+  return dexmpm_p2g_grad(b, epoch, S, Gnext, G, stream);
 }
 
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {

@@ -75,6 +75,34 @@ def footprint_bytes(specs: Sequence[EnvSpec], n_slots: int = 2, grad: bool = Fal
     return int(b)
 
 
+def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
+    """Host-side layout of a batch: particle / block / body offsets per env,
+    particle tiles (env, first particle) that never straddle envs, the owning
+    env of every grid block, and the DexEnv descriptors."""
+    envs = (N.DexEnv * len(specs))()
+    tiles, block_env, p_off, blk_off, body_off = [], [], [], [], []
+    p = blk = body = 0
+    for e, s in enumerate(specs):
+        nbx, nby, nbz = (g // 4 for g in s.grid_dim)
+        E = envs[e]
+        E.p_off, E.n, E.blk_off, E.body_off = p, s.n, blk, body
+        E.gx, E.gy, E.gz = s.grid_dim
+        E.n_bodies = s.nb
+        E.dx, E.inv_dx, E.dt, E.ground_friction = s.dx, 1.0 / s.dx, s.dt, s.ground_friction
+        E.gravity[:] = list(s.gravity)
+        E.ground_height = s.ground_height
+        p_off.append(p)
+        blk_off.append(blk)
+        body_off.append(body)
+        tiles += [(e, t) for t in range(0, s.n, tile_size)]
+        block_env += [e] * (nbx * nby * nbz)
+        p += s.n
+        blk += nbx * nby * nbz
+        body += s.nb
+    return dict(envs=envs, tiles=tiles, block_env=block_env, p_off=p_off, blk_off=blk_off, body_off=body_off,
+                n_blocks=blk, n_bodies=body, n_particles=p)
+
+
 class BatchEngine:
     def __init__(self, specs: Sequence[EnvSpec], device="cuda", tile_size: int = 128,
                  grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False):
@@ -91,28 +119,10 @@ class BatchEngine:
                 raise N.DexError(f"{s.nb} bodies > {N.MAX_BODIES} per env")
         n_real = sum(s.n for s in self.specs)
         self.n_particles = max(32, ((n_real + 31) // 32) * 32)
-        self.p_off, self.blk_off, self.body_off = [], [], []
-        envs = (N.DexEnv * len(self.specs))()
-        tiles, block_env = [], []
-        p = blk = body = 0
-        for e, s in enumerate(self.specs):
-            nbx, nby, nbz = (g // 4 for g in s.grid_dim)
-            E = envs[e]
-            E.p_off, E.n, E.blk_off, E.body_off = p, s.n, blk, body
-            E.gx, E.gy, E.gz = s.grid_dim
-            E.n_bodies = s.nb
-            E.dx, E.inv_dx, E.dt, E.ground_friction = s.dx, 1.0 / s.dx, s.dt, s.ground_friction
-            E.gravity[:] = list(s.gravity)
-            E.ground_height = s.ground_height
-            self.p_off.append(p)
-            self.blk_off.append(blk)
-            self.body_off.append(body)
-            tiles += [(e, t) for t in range(0, s.n, self.tile_size)]
-            block_env += [e] * (nbx * nby * nbz)
-            p += s.n
-            blk += nbx * nby * nbz
-            body += s.nb
-        self.n_blocks, self.n_bodies = blk, body
+        L = plan_layout(self.specs, self.tile_size)
+        self.p_off, self.blk_off, self.body_off = L["p_off"], L["blk_off"], L["body_off"]
+        envs, tiles, block_env = L["envs"], L["tiles"], L["block_env"]
+        self.n_blocks, self.n_bodies = L["n_blocks"], L["n_bodies"]
         dev = self.device
         f32 = dict(dtype=torch.float32, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)

@@ -1,0 +1,341 @@
+"""Continuous-batching request loop for rollouts and gradient rollouts.
+
+Requests (an env, a horizon in env steps, optionally a gradient) arrive over
+time.  The server admits them while their device footprint fits the HBM budget,
+keeps every admitted request's state resident on the device, and advances all
+running requests together one env step (``substeps`` substeps) per round:
+
+  * forward-phase requests (rollouts, and gradient requests before their
+    horizon) form one batch: the particle states are gathered into a
+    BatchEngine arena, stepped, and scattered back; gradient requests keep a
+    checkpoint per env step;
+  * backward-phase requests (gradient requests past their horizon) form a
+    second batch that runs one env step of the adjoint (recompute from the
+    checkpoint, reverse substeps) per round, on its own CUDA stream so that
+    it overlaps the forward batch on the device.
+
+Membership changes at round boundaries (a request that arrives while others
+run joins at the next round; a finished request leaves and frees its memory).
+Engines and their CUDA graphs are cached per membership.  Results do not depend
+on co-scheduling: envs never interact, and a request computes the same
+substeps in the same order alone or in the mix.
+"""
+from __future__ import annotations
+
+import collections
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from .engine import BatchEngine, EnvSpec, footprint_bytes, pack_poses
+
+
+@dataclass
+class Request:
+    rid: int
+    env: object                 # workloads.Env (poses for horizon * substeps substeps)
+    horizon: int                # env steps
+    grad: bool = False
+    arrival: float = 0.0        # seconds on the server clock
+    # filled by the server
+    admitted: Optional[float] = None
+    finished: Optional[float] = None
+    result: Optional[dict] = None
+    step: int = 0               # env steps done (forward), then adjoint steps done
+    phase: str = "queued"       # queued | forward | backward | done
+
+    @property
+    def spec(self) -> EnvSpec:
+        return EnvSpec.from_env(self.env)
+
+    def footprint(self, substeps):
+        return footprint_bytes([self.spec], n_slots=2, grad=self.grad, substeps=substeps,
+                               env_steps=self.horizon if self.grad else 0)
+
+
+class _Resident:
+    """Device-resident state of one admitted request."""
+
+    def __init__(self, req: Request, substeps: int, device):
+        env = req.env
+        self.n = env.n
+        f = dict(dtype=torch.float32, device=device)
+        st = env.state()
+        buf = np.zeros((24, env.n), np.float32)
+        buf[0:3], buf[3:6] = st["x"].T, st["v"].T
+        buf[6:15], buf[15:24] = st["F"].reshape(env.n, 9).T, st["C"].reshape(env.n, 9).T
+        self.state = torch.tensor(buf, **f)
+        n_sub = req.horizon * substeps
+        self.poses = torch.tensor(pack_poses(env.poses[:n_sub + 1, :, :3], env.poses[:n_sub + 1, :, 3:]), **f)
+        self.ckpt = [self.state.clone()] if req.grad else None
+        self.grad = None
+        self.bgrad = torch.zeros_like(self.poses) if req.grad else None
+
+
+class _Batch:
+    """A BatchEngine for one membership plus its per-round graphs."""
+
+    def __init__(self, reqs: List[Request], substeps: int, grad: bool, device, tile_size: int, use_graphs: bool):
+        self.ids = tuple(r.rid for r in reqs)
+        self.E = BatchEngine([r.spec for r in reqs], device=device, grad=grad, tile_size=tile_size)
+        self.T = substeps
+        nb = max(self.E.n_bodies, 1)
+        self.slot = self.E.new_slots(self.T + 1)
+        self.poses = torch.zeros((self.T + 1, nb, 8), device=device)
+        if grad:
+            self.gbuf = self.E.new_slots(2)
+            self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
+        self.use_graphs = use_graphs
+        self.graphs = {}
+
+    def _forward(self):
+        for s in range(self.T):
+            self.E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], force_clear=(s == 0))
+
+    def _backward(self):
+        self._forward()
+        E = self.E
+        g_next, g = self.gbuf[1], self.gbuf[0]
+        for s in range(self.T - 1, -1, -1):
+            E.substep_grad(self.slot[s], self.slot[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
+                           self.bgrad[s], self.bgrad[s + 1])
+            g_next, g = g, g_next
+        if self.T % 2 == 1:
+            self.gbuf[1].copy_(self.gbuf[0])
+
+    def run(self, kind: str):
+        fn = self._forward if kind == "fwd" else self._backward
+        E = self.E
+        if not self.use_graphs:
+            fn()
+            return
+        key = (kind, E.epoch & 1)
+        g = self.graphs.get(key)
+        if g is None:
+            fn()
+            e0, p0, l0 = E.epoch, E.prev_backward, E.launches
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                g.capture_begin()
+                fn()
+                g.capture_end()
+            torch.cuda.current_stream().wait_stream(side)
+            E.epoch, E.prev_backward, E.launches = e0, p0, l0
+            self.graphs[(kind, E.epoch & 1)] = g
+            return
+        g.replay()
+        E.epoch += self.T if kind == "fwd" else 2 * self.T
+        E.prev_backward = kind == "bwd"
+        E.launches += 3 * self.T if kind == "fwd" else 8 * self.T
+
+
+class Server:
+    """Continuous-batching MPM server on one GPU."""
+
+    def __init__(self, substeps=50, hbm_budget_bytes=180 * 2 ** 30, device="cuda", tile_size=128,
+                 use_graphs=True, max_cached_batches=8):
+        self.T = substeps
+        self.budget = int(hbm_budget_bytes)
+        self.device = torch.device(device)
+        self.tile_size = tile_size
+        self.use_graphs = use_graphs
+        self.queue: collections.deque = collections.deque()
+        self.running: Dict[int, Request] = {}
+        self.resident: Dict[int, _Resident] = {}
+        self.done: List[Request] = []
+        self.in_use = 0
+        self.cache: "collections.OrderedDict[tuple, _Batch]" = collections.OrderedDict()
+        self.max_cached = max_cached_batches
+        self.s_fwd = torch.cuda.Stream(device=self.device)
+        self.s_bwd = torch.cuda.Stream(device=self.device)
+        self.rounds = 0
+        self.work = 0  # particle-substeps processed
+
+    # ---------------------------------------------------------- admission
+    def submit(self, req: Request):
+        if req.footprint(self.T) > self.budget:
+            raise ValueError(f"request {req.rid} needs {req.footprint(self.T)} bytes > budget {self.budget}")
+        if req.env.poses.shape[0] < req.horizon * self.T + 1:
+            raise ValueError(f"request {req.rid}: poses for {req.horizon * self.T} substeps required")
+        req.phase = "queued"
+        self.queue.append(req)
+
+    def _admit(self, now):
+        while self.queue:
+            r = self.queue[0]
+            need = r.footprint(self.T)
+            if self.in_use + need > self.budget:
+                break
+            self.queue.popleft()
+            self.in_use += need
+            r.admitted = now
+            r.phase = "forward"
+            self.running[r.rid] = r
+            self.resident[r.rid] = _Resident(r, self.T, self.device)
+
+    def _batch(self, reqs, grad):
+        key = (grad,) + tuple(r.rid for r in reqs)
+        b = self.cache.get(key)
+        if b is None:
+            b = _Batch(reqs, self.T, grad, self.device, self.tile_size, self.use_graphs)
+            self.cache[key] = b
+            while len(self.cache) > self.max_cached:
+                self.cache.popitem(last=False)
+        else:
+            self.cache.move_to_end(key)
+        return b
+
+    # -------------------------------------------------------------- round
+    def _forward_round(self, reqs):
+        b = self._batch(reqs, grad=False)
+        E = b.E
+        for e, r in enumerate(reqs):
+            res = self.resident[r.rid]
+            o = E.p_off[e]
+            b.slot[0][:, o:o + r.env.n].copy_(res.state)
+            t0 = r.step * self.T
+            bo = E.body_off[e]
+            b.poses[:, bo:bo + r.env.nb].copy_(res.poses[t0:t0 + self.T + 1])
+        b.run("fwd")
+        for e, r in enumerate(reqs):
+            res = self.resident[r.rid]
+            o = E.p_off[e]
+            res.state.copy_(b.slot[self.T][:, o:o + r.env.n])
+            if r.grad:
+                res.ckpt.append(res.state.clone())
+            self.work += r.env.n * self.T
+
+    def _backward_round(self, reqs):
+        b = self._batch(reqs, grad=True)
+        E = b.E
+        b.gbuf[1].zero_()
+        for e, r in enumerate(reqs):
+            res = self.resident[r.rid]
+            o = E.p_off[e]
+            k = r.horizon - 1 - r.step  # env step being differentiated
+            b.slot[0][:, o:o + r.env.n].copy_(res.ckpt[k])
+            t0 = k * self.T
+            bo = E.body_off[e]
+            b.poses[:, bo:bo + r.env.nb].copy_(res.poses[t0:t0 + self.T + 1])
+            if res.grad is None:  # loss gradient of the final state: d/dx of mean |x|^2
+                res.grad = torch.zeros_like(res.state)
+                res.grad[0:3] = 2.0 * res.ckpt[-1][0:3] / r.env.n
+            b.gbuf[1][:, o:o + r.env.n].copy_(res.grad)
+        b.bgrad.zero_()
+        b.run("bwd")
+        for e, r in enumerate(reqs):
+            res = self.resident[r.rid]
+            o = E.p_off[e]
+            k = r.horizon - 1 - r.step
+            res.grad.copy_(b.gbuf[1][:, o:o + r.env.n])
+            bo = E.body_off[e]
+            t0 = k * self.T
+            res.bgrad[t0:t0 + self.T + 1] += b.bgrad[:, bo:bo + r.env.nb]
+            self.work += r.env.n * self.T
+
+    def step(self, now):
+        """Admit what fits, run one round, retire finished requests."""
+        self._admit(now)
+        fwd = [r for r in self.running.values() if r.phase == "forward"]
+        bwd = [r for r in self.running.values() if r.phase == "backward"]
+        if not fwd and not bwd:
+            return False
+        main = torch.cuda.current_stream(self.device)
+        if fwd:
+            self.s_fwd.wait_stream(main)
+            with torch.cuda.stream(self.s_fwd):
+                self._forward_round(fwd)
+        if bwd:
+            self.s_bwd.wait_stream(main)
+            with torch.cuda.stream(self.s_bwd):
+                self._backward_round(bwd)
+        main.wait_stream(self.s_fwd)
+        main.wait_stream(self.s_bwd)
+        for r in fwd:
+            r.step += 1
+            if r.step == r.horizon:
+                if r.grad:
+                    r.phase, r.step = "backward", 0
+                else:
+                    self._finish(r, now)
+        for r in bwd:
+            r.step += 1
+            if r.step == r.horizon:
+                self._finish(r, now)
+        self.rounds += 1
+        return True
+
+    def _finish(self, r, now):
+        res = self.resident[r.rid]
+        out = {"state": res.state}
+        if r.grad:
+            out["grad_state0"] = res.grad
+            out["grad_poses"] = res.bgrad
+        r.result = out
+        r.phase = "done"
+        r._finish_pending = now
+        self.done.append(r)
+        del self.running[r.rid]
+        del self.resident[r.rid]
+        self.in_use -= r.footprint(self.T)
+
+    def run(self, requests: List[Request], clock=None, max_rounds=100000):
+        """Serve requests (sorted by arrival) on a wall clock starting now;
+        returns the finished requests with latencies in seconds."""
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        rounds = 0
+        while (pending or self.queue or self.running) and rounds < max_rounds:
+            while pending and pending[0].arrival <= now():
+                self.submit(pending.popleft())
+            if not self.step(now()):
+                if pending:
+                    time.sleep(max(0.0, min(0.005, pending[0].arrival - now())))
+                continue
+            torch.cuda.current_stream(self.device).synchronize()
+            t = now()
+            for r in self.done:
+                if r.finished is None:
+                    r.finished = t
+            rounds += 1
+        return self.done
+
+
+def latency_stats(done: List[Request]):
+    lat = np.array([r.finished - r.arrival for r in done if r.finished is not None])
+    if lat.size == 0:
+        return None
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "n": int(lat.size)}
+
+
+def poisson_requests(seed=0, n=32, rate_hz=20.0, grids=(48, 64, 96), n_lo=2000, n_hi=50000, h_lo=5, h_hi=100,
+                     grad_frac=0.3, substeps=50, horizon_scale=1.0):
+    """Seeded serving workload: Poisson arrivals, grids 48/64/96^3, particles
+    log-uniform in [n_lo, n_hi], horizons uniform in [h_lo, h_hi] env steps
+    (scaled by horizon_scale), grad_frac of the requests ask for gradients."""
+    from . import workloads as W
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate_hz)
+        g = int(rng.choice(grids))
+        npart = int(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi))))
+        h = max(1, int(round(rng.integers(h_lo, h_hi + 1) * horizon_scale)))
+        grad = bool(rng.random() < grad_frac)
+        if rng.random() < 0.5:
+            env = W.make_env(seed * 100000 + i, npart, "cube", grid=g, center=(0.5, 0.16, 0.5), extent=0.18,
+                             steps=h * substeps, name=f"req{i}")
+        else:
+            env = W.make_env(seed * 100000 + i, npart, "ellipsoid", grid=g, center=(0.5, 0.13, 0.5),
+                             extent=(0.12, 0.06, 0.09), steps=h * substeps, name=f"req{i}")
+        out.append(Request(rid=i, env=env, horizon=h, grad=grad, arrival=t))
+    return out

@@ -1,0 +1,265 @@
+"""Differentiable rollouts: the hand-written adjoint behind torch.autograd.
+
+Mirror of DexDeform's mpm/torch_wrapper.py (GradModel.diff_forward,
+:107-144) with a different memory model: the reference keeps every
+substep's state (mpm/simulator.py:206) and replays substep_grad over them; here
+an env step is one autograd node (EnvStep) that saves only its input state
+(the per-env-step checkpoint) and, in backward, recomputes its T substeps from
+it into a ring buffer and runs the adjoint kernels in reverse.  The forward and
+the backward of an env step are CUDA graphs replayed on every call.
+
+Gradients flow to the input state (all 24 planes) and to the per-substep body
+poses (T+1 rows: row 0 is the pose at the env step's start, rows 1..T the
+poses the step drives), so any torch code producing the poses -- e.g. hand
+forward kinematics of joint-velocity controls -- is differentiated through.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .engine import BatchEngine, EnvSpec
+
+
+def pack_pose_tensor(pos: torch.Tensor, rot: torch.Tensor) -> torch.Tensor:
+    """(..., nb, 3), (..., nb, 4) -> (..., nb, 8) = p.xyz, 0, q.wxyz (differentiable)."""
+    return torch.cat([pos, torch.zeros_like(pos[..., :1]), rot], -1)
+
+
+class DiffSim:
+    """Differentiable batched simulator core: T substeps per env step."""
+
+    def __init__(self, specs: Sequence[EnvSpec], substeps: int, device="cuda", tile_size=128, use_graphs=True):
+        self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size)
+        self.T = int(substeps)
+        self.nb = max(self.E.n_bodies, 1)
+        self.ring = self.E.new_slots(self.T + 1)
+        self.gbuf = self.E.new_slots(2)
+        dev = self.E.device
+        self.poses = torch.zeros((self.T + 1, self.nb, 8), device=dev)
+        self.bgrad = torch.zeros((self.T + 1, self.nb, 8), device=dev)
+        self.use_graphs = use_graphs
+        self._g = {}
+
+    # eager bodies of the two graphs
+    def _fwd(self):
+        E = self.E
+        for s in range(self.T):
+            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], force_clear=(s == 0))
+
+    def _bwd(self):
+        E = self.E
+        self._fwd()
+        g_next, g = self.gbuf[1], self.gbuf[0]
+        for s in range(self.T - 1, -1, -1):
+            E.substep_grad(self.ring[s], self.ring[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
+                           self.bgrad[s], self.bgrad[s + 1])
+            g_next, g = g, g_next
+        if self.T % 2 == 1:
+            self.gbuf[1].copy_(self.gbuf[0])
+
+    def _replay(self, name, fn, epochs):
+        E = self.E
+        if not self.use_graphs:
+            fn()
+            return
+        key = (name, E.epoch & 1)
+        g = self._g.get(key)
+        if g is None:
+            fn()
+            torch.cuda.synchronize()
+            e0, p0, l0 = E.epoch, E.prev_backward, E.launches
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                g.capture_begin()
+                fn()
+                g.capture_end()
+            torch.cuda.current_stream().wait_stream(s)
+            E.epoch, E.prev_backward, E.launches = e0, p0, l0
+            self._g[(name, E.epoch & 1)] = g
+            return
+        g.replay()
+        E.epoch += epochs
+        E.prev_backward = name == "bwd"
+        E.launches += 3 * self.T if name == "fwd" else 8 * self.T
+
+    def forward(self, state: torch.Tensor, poses: torch.Tensor) -> torch.Tensor:
+        self.ring[0].copy_(state)
+        self.poses.copy_(poses)
+        self._replay("fwd", self._fwd, self.T)
+        return self.ring[self.T].clone()
+
+    def backward(self, state: torch.Tensor, poses: torch.Tensor, g_out: torch.Tensor):
+        self.ring[0].copy_(state)
+        self.poses.copy_(poses)
+        self.gbuf[1].copy_(g_out)
+        self.bgrad.zero_()
+        self._replay("bwd", self._bwd, 2 * self.T)
+        return self.gbuf[1].clone(), self.bgrad.clone()
+
+
+class EnvStep(torch.autograd.Function):
+    """state_out = T substeps of state_in under poses (T+1, nb, 8)."""
+
+    @staticmethod
+    def forward(ctx, sim: DiffSim, state: torch.Tensor, poses: torch.Tensor):
+        ctx.sim = sim
+        ctx.save_for_backward(state.detach(), poses.detach())
+        return sim.forward(state.detach(), poses.detach())
+
+    @staticmethod
+    def backward(ctx, g_out):
+        state, poses = ctx.saved_tensors
+        g_state, g_poses = ctx.sim.backward(state, poses, g_out.contiguous())
+        g_poses[..., 3] = 0.0
+        return None, g_state, g_poses
+
+
+def env_step(sim: DiffSim, state: torch.Tensor, poses: torch.Tensor) -> torch.Tensor:
+    return EnvStep.apply(sim, state, poses)
+
+
+# ------------------------------------------------------------- loss hooks
+class _Dist(torch.autograd.Function):
+    """Particle-to-body signed distances (integrator.cu:188-237) through the
+    compute_dist launcher, with its adjoint."""
+
+    @staticmethod
+    def forward(ctx, x, pos, rot, tfsr, args):
+        L = N.load()
+        n, nb = x.shape[0], pos.shape[0]
+        x, pos, rot = x.detach().contiguous(), pos.detach().contiguous(), rot.detach().contiguous()
+        d = torch.empty((n, nb), device=x.device)
+        z = torch.zeros(1, device=x.device)
+        N.check(L.compute_dist(N.ptr(x), N.ptr(pos), N.ptr(rot), N.ptr(tfsr), N.ptr(args), N.ptr(d), nb, N.ptr(z),
+                               N.ptr(z), N.ptr(z), N.ptr(z), 0, n, N.stream_ptr()), "compute_dist")
+        ctx.save_for_backward(x, pos, rot, tfsr, args)
+        return d
+
+    @staticmethod
+    def backward(ctx, gd):
+        x, pos, rot, tfsr, args = ctx.saved_tensors
+        L = N.load()
+        gx, gp, gr = torch.zeros_like(x), torch.zeros_like(pos), torch.zeros_like(rot)
+        gd = gd.contiguous()
+        N.check(L.compute_dist(N.ptr(x), N.ptr(pos), N.ptr(rot), N.ptr(tfsr), N.ptr(args), N.ptr(gd), pos.shape[0],
+                               N.ptr(gx), N.ptr(gp), N.ptr(gr), N.ptr(gd), 1, x.shape[0], N.stream_ptr()),
+                "compute_dist")
+        return gx, gp, gr, None, None
+
+
+def dists(x, pos, rot, tfsr, args):
+    return _Dist.apply(x, pos, rot, tfsr, args)
+
+
+class _GridMass(torch.autograd.Function):
+    """Grid mass of particles (integrator.cu:239-310) through particle2mass."""
+
+    @staticmethod
+    def forward(ctx, x, mass, grid_dim, dx, ids, obj):
+        L = N.load()
+        x = x.detach().contiguous()
+        g = torch.zeros(int(np.prod(grid_dim)), device=x.device)
+        gd = (ctypes.c_int * 3)(*grid_dim)
+        low = torch.zeros(3, dtype=torch.int32, device=x.device)
+        N.check(L.particle2mass(N.ptr(x), N.ptr(mass), N.ptr(low), ctypes.cast(gd, ctypes.c_void_p), dx, 1.0 / dx,
+                                N.ptr(g), N.ptr(g), N.ptr(x), N.ptr(ids), obj, 0, x.shape[0], N.stream_ptr()),
+                "particle2mass")
+        ctx.save_for_backward(x, mass, ids)
+        ctx.meta = (tuple(grid_dim), dx, obj)
+        return g.reshape(grid_dim)
+
+    @staticmethod
+    def backward(ctx, gg):
+        x, mass, ids = ctx.saved_tensors
+        grid_dim, dx, obj = ctx.meta
+        L = N.load()
+        gx = torch.zeros_like(x)
+        gg = gg.contiguous().reshape(-1)
+        gd = (ctypes.c_int * 3)(*grid_dim)
+        low = torch.zeros(3, dtype=torch.int32, device=x.device)
+        N.check(L.particle2mass(N.ptr(x), N.ptr(mass), N.ptr(low), ctypes.cast(gd, ctypes.c_void_p), dx, 1.0 / dx,
+                                N.ptr(gg), N.ptr(gg), N.ptr(gx), N.ptr(ids), obj, 1, x.shape[0], N.stream_ptr()),
+                "particle2mass")
+        return gx, None, None, None, None, None
+
+
+def grid_mass(x, mass, grid_dim, dx, ids=None, obj=-1):
+    ids = torch.zeros(x.shape[0], dtype=torch.int32, device=x.device) if ids is None else ids
+    return _GridMass.apply(x, mass, tuple(grid_dim), float(dx), ids, obj)
+
+
+# ---------------------------------------------------------------- GradModel
+class GradModel:
+    """Mirror of mpm/torch_wrapper.py:7-184 for one environment driven by a
+    hand (dexdeform_gb300.hand.SyntheticHand) under joint-velocity control.
+
+    forward(s, action) advances env step s (substeps of the DiffSim) and
+    returns the observation tuple of mpm/torch_wrapper.py:54-77:
+    (particles (n, 6 + nb) = x | v | distances to every body, tool state
+    (nb, 7), and the grid mass when return_grid is set).  loss.backward()
+    runs the adjoint through every env step (set_obs_grad is what autograd
+    does with the observation gradients)."""
+
+    def __init__(self, env, hand, substeps, return_grid=(), device="cuda", use_graphs=True):
+        self.env = env
+        self.hand = hand
+        self.device = torch.device(device)
+        self.sim = DiffSim([EnvSpec.from_env(env)], substeps, device=device, use_graphs=use_graphs)
+        E = self.sim.E
+        self.n, self.nb = env.n, env.nb
+        self.tfsr = torch.tensor(env.body_tfsr, device=self.device)
+        self.args = torch.tensor(env.body_args, device=self.device)
+        self.mass = torch.tensor(env.mass, device=self.device)
+        self.return_grid = tuple(return_grid)
+        self.substeps = substeps
+        self.zero_grad()
+
+    def zero_grad(self, return_grid=None, **kw):
+        if return_grid is not None:
+            self.return_grid = tuple(return_grid)
+        self.state = None
+        self.qpos = None
+        self.last_pose = None
+
+    def reset(self, qpos: torch.Tensor, state0: Optional[torch.Tensor] = None):
+        """Initial joint angles and particle state (SoA slot, or the env's)."""
+        E = self.sim.E
+        self.qpos = qpos
+        pos, rot = self.hand.fk(qpos)
+        self.last_pose = pack_pose_tensor(pos, rot)
+        self.state = state0 if state0 is not None else E.pack_state([self.env.state()])
+        return self.get_obs()
+
+    def particles(self, state=None):
+        st = self.state if state is None else state
+        n = self.n
+        return st[0:3, :n].t(), st[3:6, :n].t()
+
+    def get_obs(self):
+        x, v = self.particles()
+        pose = self.last_pose
+        d = dists(x.contiguous(), pose[:, :3].contiguous(), pose[:, 4:].contiguous(), self.tfsr, self.args)
+        out = [torch.cat([x, v, d], 1), torch.cat([pose[:, :3], pose[:, 4:]], 1)]
+        for _ in self.return_grid:
+            out.append(grid_mass(x.contiguous(), self.mass, self.env.grid_dim, self.env.dx))
+        return tuple(out)
+
+    def forward(self, s, action, *past_obs):
+        pos, rot, q_last = self.hand.joint_velocity_poses(self.qpos, action, self.substeps)
+        poses = torch.cat([self.last_pose[None], pack_pose_tensor(pos, rot)], 0)
+        self.state = env_step(self.sim, self.state, poses)
+        self.qpos = q_last
+        self.last_pose = poses[-1]
+        return self.get_obs()
+
+    def set_obs_grad(self, obs, grads):
+        """Add observation gradients (the reference's set_obs_grad) by
+        back-propagating them through the autograd graph."""
+        torch.autograd.backward([o for o in obs], [g for g in grads])

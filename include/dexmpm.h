@@ -197,6 +197,17 @@ int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *s, const floa
                         float *g, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
                         dexmpm_stream_t stream);
 
+/* The three kernels of dexmpm_substep_grad, callable one by one (same
+ * arguments): G2P adjoint (writes the x gradient of s and scatters
+ * dL/dv_out), grid-update adjoint (dL/d(mv), dL/dm and body-pose gradients),
+ * P2G + SVD adjoint (completes the gradient of s). */
+int dexmpm_g2p_grad(const DexBatch *b, int epoch, const float *s, const float *next_s, const float *g_next,
+                    float *g, dexmpm_stream_t stream);
+int dexmpm_grid_op_grad(const DexBatch *b, int epoch, const float *pose, const float *next_pose, float *bgrad,
+                        float *next_bgrad, dexmpm_stream_t stream);
+int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *s, const float *g_next, float *g,
+                    dexmpm_stream_t stream);
+
 /* Copy out and clear the device error word (host pointer out). */
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream);
 

@@ -1,0 +1,140 @@
+"""CPU tests: the C ABI library loads and exports what include/dexmpm.h
+declares, struct layouts agree with the header, the product's FP32 arithmetic
+(host build of mpm_math.cuh) against the FP64 oracle, and host-side logic."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, oracle_sim, rel
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "dexmpm.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    from dexdeform_gb300 import _native as N
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(native_lib, n), n
+    assert sorted(N.EXPORTED) == names
+    assert native_lib.dexmpm_version().startswith(b"dexmpm")
+
+
+def test_struct_layouts_match_header():
+    from dexdeform_gb300 import _native as N
+    src = os.path.join(tempfile.mkdtemp(), "l.c")
+    with open(src, "w") as f:
+        f.write('#include <stdio.h>\n#include <stddef.h>\n#include "dexmpm.h"\nint main(){'
+                'printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(DexEnv), offsetof(DexEnv, gravity), '
+                'sizeof(DexBatch), offsetof(DexBatch, grid), offsetof(DexBatch, block_count), '
+                'offsetof(DexBatch, error)); return 0;}\n')
+    exe = src[:-2]
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+    got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
+    want = [ctypes.sizeof(N.DexEnv), N.DexEnv.gravity.offset, ctypes.sizeof(N.DexBatch), N.DexBatch.grid.offset,
+            N.DexBatch.block_count.offset, N.DexBatch.error.offset]
+    assert got == want
+
+
+def test_product_svd_against_fp64(oracle_mod):
+    import host_math as H
+    rng = np.random.default_rng(0)
+    for scale in (0.0, 1e-4, 1e-2, 0.3, 1.0):
+        F = (np.eye(3) + rng.normal(size=(500, 3, 3)) * scale).astype(np.float32)
+        U, s, d, V, _ = H.svd(F)
+        st = np.linalg.svd(F.astype(np.float64), compute_uv=False)
+        st[:, 2] *= np.sign(np.linalg.det(F.astype(np.float64)))
+        rec = np.einsum("nij,nj,nkj->nik", U.astype(np.float64), s.astype(np.float64), V.astype(np.float64))
+        assert np.abs(rec - F).max() < 5e-6 * max(1.0, scale * 4)
+        assert np.allclose(np.linalg.det(U), 1, atol=2e-6) and np.allclose(np.linalg.det(V), 1, atol=2e-6)
+        if scale == 0.0:
+            assert (U == np.eye(3)).all() and (V == np.eye(3)).all() and (s == 1).all() and (d == 0).all()
+        else:
+            # sigma - 1 to (near) full FP32 relative precision
+            assert np.abs(d - (st - 1)).max() <= 2e-6 * np.abs(st - 1).max() + 1e-7 * (scale > 0.2)
+        # same conventions as the reference's svd3
+        oracle_mod.set_svd_mode("exact")
+        _, so, _ = oracle_mod.svd3(F.astype(np.float64))
+        oracle_mod.set_svd_mode("reference")
+        assert np.abs(s - so).max() < 1e-5 * max(1.0, 4 * scale)
+
+
+def test_product_stress_is_cancellation_free(oracle_mod):
+    """Stress from the product arithmetic vs an FP64 evaluation of the
+    reference formula 2 mu (F' - U V^T) F'^T + lam J (J-1) I."""
+    import host_math as H
+    rng = np.random.default_rng(1)
+    n = 400
+    F = (np.eye(3) + rng.normal(size=(n, 3, 3)) * 1e-3).astype(np.float32)
+    C = (rng.normal(size=(n, 3, 3)) * 0.5).astype(np.float32)
+    mly = np.tile(np.float32([2083.33, 1388.89, 50.0]), (n, 1))
+    dt = 5e-5
+    nF, P, J = H.constitutive(F, C, dt, mly)
+    Ft = np.einsum("nij,njk->nik", np.eye(3) + dt * C.astype(np.float64), F.astype(np.float64))
+    oracle_mod.set_svd_mode("exact")
+    U, s, V = oracle_mod.svd3(Ft)
+    oracle_mod.set_svd_mode("reference")
+    R = np.einsum("nij,nkj->nik", U, V)
+    Jd = np.prod(s, 1)
+    Pd = 2 * 2083.33 * np.einsum("nij,nkj->nik", Ft - R, Ft) + (1388.89 * Jd * (Jd - 1))[:, None, None] * np.eye(3)
+    assert rel(P, Pd) < 1e-5
+    assert rel(J, Jd) < 1e-7
+
+
+def test_host_substep_matches_oracle_off_rest(oracle_mod):
+    """The product arithmetic (host build) for one substep from a non-rest
+    state meets the 1e-5 bar against the FP64 oracle."""
+    import host_math as H
+    from dexdeform_gb300 import workloads as W
+    env = W.tiny_env(0, n=256, grid=32, nb=6, steps=2, dt=1e-4)
+    st = W.perturb_state(env, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+    oracle_mod.set_svd_mode("exact")
+    a = oracle_sim(oracle_mod, env).substep(st, env.pose(0), env.pose(1))
+    oracle_mod.set_svd_mode("reference")
+    b = H.substep(env, st, 0)
+    for k in ("x", "v", "F", "C"):
+        assert rel(b[k], a[k]) < 1e-5, k
+
+
+def test_layout_plan_and_footprint():
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import EnvSpec, footprint_bytes, plan_layout
+    envs = W.batch_envs(0, n_envs=7, steps=2, n_lo=100, n_hi=900)
+    specs = [EnvSpec.from_env(e) for e in envs]
+    for tile in (64, 128, 256):
+        L = plan_layout(specs, tile)
+        seen = np.zeros(sum(s.n for s in specs), np.int32)
+        for e, first in L["tiles"]:
+            n = min(tile, specs[e].n - first)
+            assert 0 <= first < specs[e].n and n > 0
+            seen[L["p_off"][e] + first:L["p_off"][e] + first + n] += 1
+        assert (seen == 1).all()
+        assert len(L["block_env"]) == sum((s.grid_dim[0] // 4) ** 3 for s in specs)
+        assert all(L["block_env"][L["blk_off"][e]] == e for e in range(len(specs)))
+    a = footprint_bytes(specs)
+    b = footprint_bytes(specs, grad=True, substeps=50, env_steps=10)
+    assert 0 < a < b
+
+
+def test_workloads_are_seeded_and_in_range():
+    from dexdeform_gb300 import workloads as W
+    a, b = W.batch_envs(0, n_envs=16, steps=5), W.batch_envs(0, n_envs=16, steps=5)
+    assert all(np.array_equal(x.x, y.x) and np.array_equal(x.poses, y.poses) for x, y in zip(a, b))
+    counts = np.array([e.n for e in a])
+    assert counts.min() >= 2000 and counts.max() <= 30000
+    for e in a:
+        assert 30.0 <= e.mu_lam_yield[0, 2] <= 80.0
+        r, h = e.body_args[:, 0], e.body_args[:, 1]
+        assert (r >= 0.008).all() and (r <= 0.02).all() and (h >= 0.02).all() and (h <= 0.05).all()
+        v = np.linalg.norm(np.diff(e.poses[:, :, :3], axis=0), axis=-1) / e.dt
+        assert v.max() <= 0.5 + 1e-3
+        q = np.linalg.norm(e.poses[:, :, 3:], axis=-1)
+        assert np.abs(q - 1).max() < 1e-5

@@ -1,0 +1,144 @@
+"""Differentiable rollouts on the GPU: the EnvStep autograd node (per-env-step
+checkpoint + substep recomputation + hand-written adjoint) against the FP64
+oracle's chained adjoint, and against central finite differences."""
+import numpy as np
+import pytest
+
+from conftest import oracle_sim, rel
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def cuda(native_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return native_lib
+
+
+def _sim(env, T, graphs=True):
+    from dexdeform_gb300.engine import EnvSpec
+    from dexdeform_gb300.torch_wrapper import DiffSim
+    return DiffSim([EnvSpec.from_env(env)], T, use_graphs=graphs)
+
+
+def _poses(env, t0, T):
+    from dexdeform_gb300.engine import pack_poses
+    return torch.tensor(pack_poses(env.poses[t0:t0 + T + 1, :, :3], env.poses[t0:t0 + T + 1, :, 3:]), device="cuda")
+
+
+def test_env_step_adjoint_matches_oracle_chain(cuda, oracle_mod):
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.torch_wrapper import env_step
+    T = 4
+    env = W.tiny_env(1, n=256, grid=32, nb=6, steps=T, dt=1e-4)
+    st = W.perturb_state(env, seed=3, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+    sim = _sim(env, T)
+    E = sim.E
+    s0 = E.pack_state([st]).requires_grad_(True)
+    poses = _poses(env, 0, T).requires_grad_(True)
+    rng = np.random.default_rng(0)
+    wts = {k: rng.normal(size=st[k].shape).astype(np.float32) for k in st}
+    W_t = E.pack_state([wts])
+    out = env_step(sim, s0, poses)
+    (out * W_t).sum().backward()
+    g_gpu = E.unpack_state(s0.grad)[0]
+    pg = poses.grad.cpu().numpy()
+    # oracle: forward storing every state, then the chained substep adjoints
+    o = oracle_sim(oracle_mod, env)
+    states = [st]
+    for t in range(T):
+        states.append(o.substep(states[-1], env.pose(t), env.pose(t + 1)))
+    g = {k: wts[k].astype(np.float64) for k in wts}
+    bp = np.zeros((T + 1, env.nb, 3))
+    br = np.zeros((T + 1, env.nb, 4))
+    for t in range(T - 1, -1, -1):
+        g, (a, b), (c, d) = o.substep_grad(states[t], env.pose(t), env.pose(t + 1), states[t + 1]["v"], g)
+        bp[t] += a
+        br[t] += b
+        bp[t + 1] += c
+        br[t + 1] += d
+    for k in ("x", "v", "F", "C"):
+        assert rel(g_gpu[k], g[k]) < 1e-3, k
+    assert rel(pg[:, :, :3], bp) < 1e-3
+    assert rel(pg[:, :, 4:], br) < 1e-3
+
+
+def test_env_step_directional_finite_difference(cuda):
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.torch_wrapper import env_step
+    T = 8
+    env = W.tiny_env(2, n=512, grid=32, nb=6, steps=T, dt=1e-4)
+    st = W.perturb_state(env, seed=4, v_scale=0.2, c_scale=1.0, f_scale=0.01)
+    sim = _sim(env, T)
+    E = sim.E
+    s0 = E.pack_state([st])
+    poses = _poses(env, 0, T)
+    tgt = s0[0:3].clone() + 0.01
+
+    def loss(s):
+        out = env_step(sim, s, poses)
+        return ((out[0:3] - tgt) ** 2).double().sum() + (out[3:6] ** 2).double().sum() * 1e-3
+
+    s = s0.clone().requires_grad_(True)
+    loss(s).backward()
+    rng = np.random.default_rng(1)
+    d = torch.zeros_like(s0)
+    d[3:6] = torch.tensor(rng.normal(size=(3, s0.shape[1])), dtype=torch.float32, device="cuda")
+    d[:, env.n:] = 0
+    eps = 1e-3
+    with torch.no_grad():
+        fd = (loss(s0 + eps * d) - loss(s0 - eps * d)) / (2 * eps)
+    an = (s.grad.double() * d.double()).sum()
+    assert abs(float(fd) - float(an)) < 2e-2 * abs(float(an)) + 1e-9
+
+
+def test_controls_gradient_by_central_differences(cuda):
+    """Config-1 style: joint-velocity controls -> hand FK -> capsule poses ->
+    MPM; gradient of a particle-to-target loss wrt the controls against
+    central differences (eps = 1e-3) on 16 random control coordinates."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.hand import N_BODIES, SyntheticHand, default_qpos
+    from dexdeform_gb300.torch_wrapper import GradModel
+    hand = SyntheticHand(base_pos=(0.5, 0.2, 0.47), action_scale=0.05)
+    env = W.make_env(7, 3000, "ellipsoid", grid=64, dt=5e-5, center=(0.5, 0.11, 0.5), extent=(0.12, 0.06, 0.09),
+                     nb=N_BODIES, steps=2, name="diff-small")
+    env.body_tfsr, env.body_args = hand.body_shapes()
+    S, T = 3, 10
+    rng = np.random.default_rng(0)
+    actions = torch.tensor(rng.normal(scale=0.1, size=(S, 24)), dtype=torch.float32, device="cuda")
+    target = torch.tensor(env.x + rng.normal(scale=0.01, size=env.x.shape).astype(np.float32), device="cuda")
+    model = GradModel(env, hand, T)
+    q0 = default_qpos()
+
+    def rollout(acts):
+        model.zero_grad()
+        model.reset(q0)
+        for s in range(S):
+            obs = model.forward(s, acts[s])
+        x = obs[0][:, :3]
+        return ((x - target) ** 2).sum(1).double().mean()
+
+    a = actions.clone().requires_grad_(True)
+    L = rollout(a)
+    L.backward()
+    grad = a.grad.clone()
+    idx = rng.choice(S * 24, size=16, replace=False)
+    eps = 1e-3
+    errs = []
+    with torch.no_grad():
+        for i in idx:
+            e = torch.zeros(S * 24, device="cuda")
+            e[i] = eps
+            e = e.reshape(S, 24)
+            fd = (rollout(actions + e) - rollout(actions - e)) / (2 * eps)
+            an = grad.reshape(-1)[i]
+            errs.append((float(fd), float(an)))
+    fd = np.array([f for f, _ in errs])
+    an = np.array([g for _, g in errs])
+    scale = np.abs(an).max()
+    assert scale > 0
+    # componentwise agreement relative to the gradient's scale
+    assert np.abs(fd - an).max() < 5e-2 * scale, errs
+    assert np.corrcoef(fd, an)[0, 1] > 0.99
