@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libdexmpm.so")
 
 OK, ERR_ARG, ERR_LAUNCH, ERR_OUT_OF_GRID, ERR_TOO_MANY_BODIES = 0, 1, 2, 4, 8
 MAX_BODIES = 32
+FLAG_EXACT_CAPSULE_GRAD = 1
 STATE_PLANES = 24
 PX, PV, PF, PC = 0, 3, 6, 15
 

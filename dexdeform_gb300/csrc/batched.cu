@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
         load_pose(pose, E.body_off + b, cur);
         load_pose(next_pose, E.body_off + b, nxt);
         load_shape(B.body_shape, E.body_off + b, sh);
-        contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn);
+        contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn, (B.reserved & DEXMPM_FLAG_EXACT_CAPSULE_GRAD) != 0);
       }
 #pragma unroll
       for (int c = 0; c < 7; ++c) {

@@ -212,9 +212,12 @@ DX_HD f3 shape_grad(qf tfsr, qf args, f3 g) {
   return grad;
 }
 // shape.h:104-152.  The reference's capsule branch back-propagates its own
-// zero-initialised accumulator instead of grad_out, so it always returns 0;
-// that behaviour is kept for gradient parity.
-DX_HD f3 shape_grad_backward(qf tfsr, qf args, f3 g, f3 gout) {
+// zero-initialised accumulator instead of grad_out, so it always returns 0
+// (the capsule-normal term of the pose gradient is dropped); that behaviour is
+// the default, for gradient parity.  exact_capsule = true gives the true
+// derivative of normalized(p2(g)) instead, where p2.y does not depend on g.y
+// inside the segment span.
+DX_HD f3 shape_grad_backward(qf tfsr, qf args, f3 g, f3 gout, bool exact_capsule = false) {
   int type = shape_type(tfsr);
   f3 gin = mk3(0.f, 0.f, 0.f);
   if (type == 0) {
@@ -231,6 +234,14 @@ DX_HD f3 shape_grad_backward(qf tfsr, qf args, f3 g, f3 gout) {
       if (q.z < 0) gin.z = 0.f;
       abs_backward(g, gin);
     }
+  } else if (type == 1 && exact_capsule) {
+    float h = args.x;
+    f3 p2 = g;
+    p2.y += h * 0.5f;
+    bool inside = p2.y >= 0.f && p2.y <= h;
+    p2.y -= fminf(fmaxf(p2.y, 0.f), h);
+    gin = vnormalized_backward(p2, gout);
+    if (inside) gin.y = 0.f;
   }
   return gin;
 }
@@ -554,7 +565,7 @@ DX_HD f3 boundary_backward(f3 gv, f3 vv, int gx, int gy, int gz, int Gx, int Gy,
 // leaving it and is replaced by the gradient of vo.  Pose gradients are added
 // to g_cur (pos 3 + quat 4) and g_nxt.
 DX_HD void contact_backward(f3 gx, f3 vo, f3 &gv, const BodyPose &cur, const BodyPose &nxt, const BodyShape &sh,
-                            float dt, float g_cur[7], float g_nxt[7]) {
+                            float dt, float g_cur[7], float g_nxt[7], bool exact_capsule = false) {
   float friction = sh.tfsr.x, softness = sh.tfsr.y;
   f3 gxb = xform_inv(cur.p, cur.q, gx);
   float dist = shape_sdf(sh.tfsr, sh.args, gxb);
@@ -603,7 +614,7 @@ DX_HD void contact_backward(f3 gx, f3 vo, f3 &gv, const BodyPose &cur, const Bod
   g_nxt[3] += g_nq.w; g_nxt[4] += g_nq.x; g_nxt[5] += g_nq.y; g_nxt[6] += g_nq.z;
   f3 g_rn = mk3(0.f, 0.f, 0.f);
   qrot_backward(cur.q, rn, g_n, g_bq, g_rn);
-  g_gxb += shape_grad_backward(sh.tfsr, sh.args, gxb, vnormalized_backward(un, g_rn));
+  g_gxb += shape_grad_backward(sh.tfsr, sh.args, gxb, vnormalized_backward(un, g_rn), exact_capsule);
   float ed = expf(-dist * softness);
   if (ed <= 1.f) g_gxb += un * (-softness * ed * g_infl);
   f3 g_tmp = mk3(0.f, 0.f, 0.f);

@@ -105,7 +105,10 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
 
 class BatchEngine:
     def __init__(self, specs: Sequence[EnvSpec], device="cuda", tile_size: int = 128,
-                 grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False):
+                 grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False,
+                 capsule_grad: str = "reference"):
+        """capsule_grad: "reference" drops the capsule-normal term of the body
+        pose gradient as the reference does; "exact" keeps it."""
         N.require_cuda()
         self.lib = N.load()
         self.device = torch.device(device)
@@ -162,6 +165,8 @@ class BatchEngine:
         b = N.DexBatch()
         b.n_envs, b.n_particles, b.n_tiles, b.n_blocks = len(self.specs), Np, len(tiles), self.n_blocks
         b.n_bodies, b.tile_size, b.grid_ctas = self.n_bodies, self.tile_size, self.grid_ctas
+        assert capsule_grad in ("reference", "exact")
+        b.reserved = N.FLAG_EXACT_CAPSULE_GRAD if capsule_grad == "exact" else 0
         b.envs, b.tiles, b.block_env = self.envs_t.data_ptr(), self.tiles_t.data_ptr(), self.block_env_t.data_ptr()
         b.mass, b.vol, b.mu_lam_yield = self.mass.data_ptr(), self.vol.data_ptr(), self.mly.data_ptr()
         for k in range(2):

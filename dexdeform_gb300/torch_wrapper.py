@@ -33,8 +33,9 @@ def pack_pose_tensor(pos: torch.Tensor, rot: torch.Tensor) -> torch.Tensor:
 class DiffSim:
     """Differentiable batched simulator core: T substeps per env step."""
 
-    def __init__(self, specs: Sequence[EnvSpec], substeps: int, device="cuda", tile_size=128, use_graphs=True):
-        self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size)
+    def __init__(self, specs: Sequence[EnvSpec], substeps: int, device="cuda", tile_size=128, use_graphs=True,
+                 capsule_grad="reference"):
+        self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size, capsule_grad=capsule_grad)
         self.T = int(substeps)
         self.nb = max(self.E.n_bodies, 1)
         self.ring = self.E.new_slots(self.T + 1)
@@ -207,11 +208,13 @@ class GradModel:
     runs the adjoint through every env step (set_obs_grad is what autograd
     does with the observation gradients)."""
 
-    def __init__(self, env, hand, substeps, return_grid=(), device="cuda", use_graphs=True):
+    def __init__(self, env, hand, substeps, return_grid=(), device="cuda", use_graphs=True,
+                 capsule_grad="reference"):
         self.env = env
         self.hand = hand
         self.device = torch.device(device)
-        self.sim = DiffSim([EnvSpec.from_env(env)], substeps, device=device, use_graphs=use_graphs)
+        self.sim = DiffSim([EnvSpec.from_env(env)], substeps, device=device, use_graphs=use_graphs,
+                           capsule_grad=capsule_grad)
         E = self.sim.E
         self.n, self.nb = env.n, env.nb
         self.tfsr = torch.tensor(env.body_tfsr, device=self.device)

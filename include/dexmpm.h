@@ -145,9 +145,13 @@ typedef struct {
   float ground_height; /* cells; the particle clamp is [gh*dx, (G-3)*dx] */
 } DexEnv;              /* 64 bytes */
 
+/* DexBatch.flags bits */
+#define DEXMPM_FLAG_EXACT_CAPSULE_GRAD 1 /* true capsule-normal derivative in the grid adjoint; the
+                                            reference drops it (mpm/csrc/shape.h:138-148) */
+
 typedef struct {
   int32_t n_envs, n_particles, n_tiles, n_blocks;
-  int32_t n_bodies, tile_size, grid_ctas, reserved;
+  int32_t n_bodies, tile_size, grid_ctas, reserved; /* reserved = flags (DEXMPM_FLAG_*) */
   const DexEnv *envs;         /* [n_envs] */
   const int32_t *tiles;       /* [n_tiles][2]: env, first particle within the env */
   const int32_t *block_env;   /* [n_blocks]: owning env */

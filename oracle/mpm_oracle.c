@@ -171,6 +171,12 @@ static v3 shape_grad(qt tfsr, qt args, v3 g) {
   return grad;
 }
 
+/* Capsule-normal derivative: 0 restates the reference (below), 1 gives the
+   true derivative (not part of the reference; used to test the product's
+   optional exact mode). */
+static int g_capsule_exact = 0;
+void orc_set_capsule_grad(int exact) { g_capsule_exact = exact; }
+
 /* shape.h:104-152.  The capsule branch back-propagates a zero vector (it reads
    grad_in, which is still zero, instead of grad_out), so it always returns 0. */
 static v3 shape_grad_backward(qt tfsr, qt args, v3 g, v3 gout) {
@@ -197,6 +203,11 @@ static v3 shape_grad_backward(qt tfsr, qt args, v3 g, v3 gout) {
     p2.y += h / 2;
     double zero_y = (p2.y >= 0.0 && p2.y <= h) ? 1.0 : 0.0;
     p2.y -= fmin(fmax(p2.y, 0.0), h);
+    if (g_capsule_exact) {
+      gin = vnormalized_backward(p2, gout);
+      if (zero_y != 0.0) gin.y = 0.0;
+      return gin;
+    }
     gin = vnormalized_backward(p2, gin);
     gin.y *= zero_y;
     return gin;

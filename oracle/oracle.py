@@ -314,3 +314,9 @@ def set_svd_mode(mode: str):
     """``"reference"`` (default): the reference's svd3 restated exactly.
     ``"exact"``: converged FP64 Jacobi with the same conventions."""
     _load(ORACLE_SO).orc_set_svd_mode(ctypes.c_int({"reference": 0, "exact": 1}[mode]))
+
+
+def set_capsule_grad(mode: str):
+    """``"reference"`` (default): the reference's capsule adjoint, which drops
+    the capsule-normal term.  ``"exact"``: its true derivative."""
+    _load(ORACLE_SO).orc_set_capsule_grad(ctypes.c_int({"reference": 0, "exact": 1}[mode]))

@@ -17,10 +17,10 @@ def cuda(native_lib):
     return native_lib
 
 
-def _sim(env, T, graphs=True):
+def _sim(env, T, graphs=True, capsule_grad="reference"):
     from dexdeform_gb300.engine import EnvSpec
     from dexdeform_gb300.torch_wrapper import DiffSim
-    return DiffSim([EnvSpec.from_env(env)], T, use_graphs=graphs)
+    return DiffSim([EnvSpec.from_env(env)], T, use_graphs=graphs, capsule_grad=capsule_grad)
 
 
 def _poses(env, t0, T):
@@ -66,32 +66,35 @@ def test_env_step_adjoint_matches_oracle_chain(cuda, oracle_mod):
 
 
 def test_env_step_directional_finite_difference(cuda):
+    """Directional derivative along a random perturbation of the particle
+    positions.  The state is FP32, so the perturbation (2e-4, ~1e-2 cells) is
+    chosen well above its rounding and the loss is accumulated in FP64."""
     from dexdeform_gb300 import workloads as W
     from dexdeform_gb300.torch_wrapper import env_step
     T = 8
     env = W.tiny_env(2, n=512, grid=32, nb=6, steps=T, dt=1e-4)
     st = W.perturb_state(env, seed=4, v_scale=0.2, c_scale=1.0, f_scale=0.01)
-    sim = _sim(env, T)
+    sim = _sim(env, T, capsule_grad="exact")
     E = sim.E
     s0 = E.pack_state([st])
     poses = _poses(env, 0, T)
-    tgt = s0[0:3].clone() + 0.01
+    tgt = s0[0:3].double() + 0.01
 
     def loss(s):
-        out = env_step(sim, s, poses)
-        return ((out[0:3] - tgt) ** 2).double().sum() + (out[3:6] ** 2).double().sum() * 1e-3
+        out = env_step(sim, s, poses).double()
+        return ((out[0:3] - tgt) ** 2).sum() + (out[3:6] ** 2).sum() * 1e-3
 
     s = s0.clone().requires_grad_(True)
     loss(s).backward()
     rng = np.random.default_rng(1)
     d = torch.zeros_like(s0)
-    d[3:6] = torch.tensor(rng.normal(size=(3, s0.shape[1])), dtype=torch.float32, device="cuda")
+    d[0:3] = torch.tensor(rng.normal(size=(3, s0.shape[1])), dtype=torch.float32, device="cuda")
     d[:, env.n:] = 0
-    eps = 1e-3
+    eps = 2e-4
     with torch.no_grad():
         fd = (loss(s0 + eps * d) - loss(s0 - eps * d)) / (2 * eps)
     an = (s.grad.double() * d.double()).sum()
-    assert abs(float(fd) - float(an)) < 2e-2 * abs(float(an)) + 1e-9
+    assert abs(float(fd) - float(an)) < 1e-2 * abs(float(an))
 
 
 def test_controls_gradient_by_central_differences(cuda):
@@ -109,7 +112,10 @@ def test_controls_gradient_by_central_differences(cuda):
     rng = np.random.default_rng(0)
     actions = torch.tensor(rng.normal(scale=0.1, size=(S, 24)), dtype=torch.float32, device="cuda")
     target = torch.tensor(env.x + rng.normal(scale=0.01, size=env.x.shape).astype(np.float32), device="cuda")
-    model = GradModel(env, hand, T)
+    # the exact capsule-normal derivative: the reference's adjoint drops that
+    # term (mpm/csrc/shape.h:138-148), so only the exact mode can match
+    # finite differences when capsules drive the object
+    model = GradModel(env, hand, T, capsule_grad="exact")
     q0 = default_qpos()
 
     def rollout(acts):
@@ -117,8 +123,8 @@ def test_controls_gradient_by_central_differences(cuda):
         model.reset(q0)
         for s in range(S):
             obs = model.forward(s, acts[s])
-        x = obs[0][:, :3]
-        return ((x - target) ** 2).sum(1).double().mean()
+        x = obs[0][:, :3].double()
+        return ((x - target.double()) ** 2).sum(1).mean()
 
     a = actions.clone().requires_grad_(True)
     L = rollout(a)
@@ -142,3 +148,32 @@ def test_controls_gradient_by_central_differences(cuda):
     # componentwise agreement relative to the gradient's scale
     assert np.abs(fd - an).max() < 5e-2 * scale, errs
     assert np.corrcoef(fd, an)[0, 1] > 0.99
+
+
+def test_exact_capsule_adjoint_matches_oracle(cuda, oracle_mod):
+    """The optional exact capsule-normal derivative against the oracle's."""
+    import os
+    from conftest import GOLDEN, golden_env
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec, pack_poses
+    env, z = golden_env(os.path.join(GOLDEN, "ref_grad_32.npz"))
+    E = BatchEngine([EnvSpec.from_env(env)], grad=True, capsule_grad="exact")
+    poses = torch.tensor(pack_poses(env.poses[:, :, :3], env.poses[:, :, 3:]), device="cuda")
+    st = {k: z[f"in_{k}"] for k in ("x", "v", "F", "C")}
+    s0 = E.pack_state([st])
+    s1 = E.new_slots(1)[0]
+    E.substep(s0, s1, poses[0], poses[1])
+    gn = E.pack_state([{k: z[f"gnext_{k}"] for k in ("x", "v", "F", "C")}])
+    g = E.new_slots(1)[0]
+    bg = torch.zeros((2, E.n_bodies, 8), device="cuda")
+    E.substep_grad(s0, s1, gn, g, poses[0], poses[1], bg[0], bg[1])
+    oracle_mod.set_capsule_grad("exact")
+    try:
+        o = oracle_sim(oracle_mod, env)
+        nx = o.substep(st, env.pose(0), env.pose(1))
+        og, (bp, br), (nbp, nbr) = o.substep_grad(st, env.pose(0), env.pose(1), nx["v"],
+                                                  {k: z[f"gnext_{k}"] for k in ("x", "v", "F", "C")})
+    finally:
+        oracle_mod.set_capsule_grad("reference")
+    b = bg.cpu().numpy()
+    assert rel(b[0, :, :3], bp) < 1e-3 and rel(b[0, :, 4:], br) < 1e-3
+    assert rel(b[1, :, :3], nbp) < 1e-3 and rel(b[1, :, 4:], nbr) < 1e-3

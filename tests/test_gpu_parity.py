@@ -262,8 +262,11 @@ def test_graph_replay_equals_eager(cuda):
             g0 = R.backward(g).clone()
         outs.append((fin, g0, R.bgrad.clone()))
         assert E.error_word() == 0
-    for a, b in zip(outs[0], outs[1]):
-        assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
+    # states agree to FP32 rounding; gradients carry the run-to-run float
+    # atomic ordering of the scatters, amplified by the SVD adjoint's
+    # 1/(sigma_j^2 - sigma_i^2) factors near rest
+    for (a, b), tol in zip(zip(outs[0], outs[1]), (1e-5, 5e-4, 5e-4)):
+        assert rel(a.cpu().numpy(), b.cpu().numpy()) < tol
 
 
 def test_full_batch_properties(cuda):

@@ -39,7 +39,10 @@ def test_mixed_results_equal_alone(cuda):
         for k in alone:
             a, b = alone[k].cpu().numpy(), mixed[r.rid][k].cpu().numpy()
             assert np.isfinite(a).all()
-            assert rel(b, a) < 1e-5, (r.rid, k)
+            # states to FP32 rounding; gradients within the run-to-run
+            # float-atomic ordering noise of the adjoint (also seen alone vs
+            # alone)
+            assert rel(b, a) < (1e-5 if k == "state" else 5e-4), (r.rid, k)
 
 
 def test_admission_respects_budget(cuda):
