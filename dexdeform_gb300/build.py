@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libdexmpm.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["batched.cu", "ref_abi.cu"]
+SOURCES = ["batched.cu", "ref_abi.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

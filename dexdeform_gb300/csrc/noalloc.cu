@@ -1,0 +1,158 @@
+// noalloc.cu -- one forward substep of one environment without any device
+// allocation by this library or by the caller.
+//
+// Some callers cannot call cudaMalloc.  A host application may own nearly all
+// device memory through its own pool allocator and forbid allocations from
+// plugins (runtimes that reserve most of the GPU up front do this), and a
+// real-time control loop may not be allowed to block on, or fail in, an
+// allocation in the middle of an episode.  Such callers pass only their
+// inputs and outputs; the grids, active-block lists and counters the substep
+// needs live in one file-scope device array of fixed size, below.
+//
+// Limits of that array: grids up to 262,144 cells (64^3, the reference's
+// default domain) and up to 1,048,576 particles, 32 bodies.  It takes 12.7 MB
+// on every GPU that loads this part of the library, held until the process
+// exits (with CUDA's default lazy module loading that happens on the first
+// call on a device).
+//
+// Every call shares the array and leaves its contents behind; each call
+// clears what must start at zero before it runs.  Calls whose work overlaps on
+// the GPU (different streams or threads, no ordering between them) race on the
+// array and give wrong results: order them on one stream.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "../../include/dexmpm.h"
+
+namespace {
+
+constexpr int kMaxCells = 64 * 64 * 64;
+constexpr int kMaxBlocks = kMaxCells / 64;
+constexpr int kMaxParticles = 1 << 20;
+constexpr int kTile = 128;
+constexpr int kMaxTiles = kMaxParticles / kTile;
+
+// byte offsets inside the array (each region 256-byte aligned)
+constexpr size_t kGrid0 = 0;
+constexpr size_t kGrid1 = kGrid0 + (size_t)kMaxCells * 16;
+constexpr size_t kVout = kGrid1 + (size_t)kMaxCells * 16;
+constexpr size_t kFlag0 = kVout + (size_t)kMaxCells * 16;
+constexpr size_t kFlag1 = kFlag0 + (size_t)kMaxBlocks * 4;
+constexpr size_t kList0 = kFlag1 + (size_t)kMaxBlocks * 4;
+constexpr size_t kList1 = kList0 + (size_t)kMaxBlocks * 4;
+constexpr size_t kBlockEnv = kList1 + (size_t)kMaxBlocks * 4;
+constexpr size_t kTiles = kBlockEnv + (size_t)kMaxBlocks * 4;
+constexpr size_t kEnv = kTiles + (size_t)kMaxTiles * 8;
+constexpr size_t kCounts = kEnv + 256;  // block_count[2], done_counter, error
+constexpr size_t kBytes = kCounts + 256;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
+
+std::mutex g_mutex;
+void *g_addr[64] = {nullptr};  // per device ordinal
+
+// Device address of the array for the current device (host code only has a
+// stand-in symbol; the address must come from the runtime).
+int scratch_address(void **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEXMPM_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (g_addr[dev] == nullptr) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return DEXMPM_ERR_LAUNCH;
+    g_addr[dev] = p;
+  }
+  *out = g_addr[dev];
+  return DEXMPM_OK;
+}
+
+// Writes the env descriptor, the tiles and the block->env table, and zeroes
+// the flags, list counts, ticket and (when no caller word is given) the error
+// word used by this call.
+__global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks, int32_t *caller_error) {
+  unsigned char *base = g_noalloc_scratch;
+  int32_t *tiles = reinterpret_cast<int32_t *>(base + kTiles);
+  int32_t *block_env = reinterpret_cast<int32_t *>(base + kBlockEnv);
+  uint32_t *flag0 = reinterpret_cast<uint32_t *>(base + kFlag0);
+  uint32_t *flag1 = reinterpret_cast<uint32_t *>(base + kFlag1);
+  int stride = gridDim.x * blockDim.x;
+  int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int t = t0; t < n_tiles; t += stride) {
+    tiles[2 * t] = 0;
+    tiles[2 * t + 1] = t * kTile;
+  }
+  for (int b = t0; b < n_blocks; b += stride) {
+    block_env[b] = 0;
+    flag0[b] = 0u;
+    flag1[b] = 0u;
+  }
+  if (t0 == 0) {
+    *reinterpret_cast<DexEnv *>(base + kEnv) = env;
+    int32_t *counts = reinterpret_cast<int32_t *>(base + kCounts);
+    counts[0] = 0;
+    counts[1] = 0;
+    counts[2] = 0;  // done_counter
+    if (caller_error == nullptr) counts[3] = 0;
+  }
+}
+
+}  // namespace
+
+extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *next_s, const float *mass,
+                                      const float *vol, const float *mu_lam_yield, const float *body_shape,
+                                      const float *pose, const float *next_pose, int32_t *error,
+                                      dexmpm_stream_t stream) {
+  if (!env || !s || !next_s || !mass || !vol || !mu_lam_yield) return DEXMPM_ERR_ARG;
+  const DexEnv e = *env;
+  if (e.p_off != 0 || e.blk_off != 0 || e.body_off != 0 || e.n < 0 || e.n > kMaxParticles) return DEXMPM_ERR_ARG;
+  if (e.gx < 8 || e.gy < 8 || e.gz < 8 || (e.gx & 3) || (e.gy & 3) || (e.gz & 3)) return DEXMPM_ERR_ARG;
+  if ((long long)e.gx * e.gy * e.gz > kMaxCells) return DEXMPM_ERR_ARG;
+  if (e.n_bodies < 0 || e.n_bodies > DEXMPM_MAX_BODIES) return DEXMPM_ERR_ARG;
+  if (e.n_bodies > 0 && (!body_shape || !pose || !next_pose)) return DEXMPM_ERR_ARG;
+  void *addr = nullptr;
+  int rc = scratch_address(&addr);
+  if (rc) return rc;
+  unsigned char *base = static_cast<unsigned char *>(addr);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n_blocks = (e.gx / 4) * (e.gy / 4) * (e.gz / 4);
+  const int n_tiles = (e.n + kTile - 1) / kTile;
+  // the P2G target grid of this call must start at zero
+  if (cudaMemsetAsync(base + kGrid0, 0, (size_t)n_blocks * 64 * 16, st) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  const int threads = 256, work = n_blocks > n_tiles ? n_blocks : n_tiles;
+  const int blocks = (work + threads - 1) / threads > 0 ? (work + threads - 1) / threads : 1;
+  k_noalloc_setup<<<blocks, threads, 0, st>>>(e, n_tiles, n_blocks, error);
+  if (cudaGetLastError() != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+
+  DexBatch b;
+  b.n_envs = 1;
+  b.n_particles = e.n > 0 ? e.n : 1;
+  b.n_tiles = n_tiles;
+  b.n_blocks = n_blocks;
+  b.n_bodies = e.n_bodies;
+  b.tile_size = kTile;
+  b.grid_ctas = 152 * 4;
+  b.reserved = 0;
+  b.envs = reinterpret_cast<const DexEnv *>(base + kEnv);
+  b.tiles = reinterpret_cast<const int32_t *>(base + kTiles);
+  b.block_env = reinterpret_cast<const int32_t *>(base + kBlockEnv);
+  b.mass = mass;
+  b.vol = vol;
+  b.mu_lam_yield = mu_lam_yield;
+  b.grid[0] = reinterpret_cast<float *>(base + kGrid0);
+  b.grid[1] = reinterpret_cast<float *>(base + kGrid1);
+  b.vout = reinterpret_cast<float *>(base + kVout);
+  b.vout_grad[0] = b.vout_grad[1] = nullptr;
+  b.in_grad[0] = b.in_grad[1] = nullptr;
+  b.block_flag[0] = reinterpret_cast<uint32_t *>(base + kFlag0);
+  b.block_flag[1] = reinterpret_cast<uint32_t *>(base + kFlag1);
+  b.block_list[0] = reinterpret_cast<int32_t *>(base + kList0);
+  b.block_list[1] = reinterpret_cast<int32_t *>(base + kList1);
+  b.block_count = reinterpret_cast<int32_t *>(base + kCounts);
+  b.done_counter = reinterpret_cast<uint32_t *>(base + kCounts + 8);
+  b.body_shape = body_shape;
+  b.error = error ? error : reinterpret_cast<int32_t *>(base + kCounts + 12);
+  // epoch 0: P2G into grid 0; the grid update finds list 1 empty
+  return dexmpm_substep(&b, 0, s, next_s, pose, next_pose, 0, stream);
+}

@@ -212,6 +212,27 @@ int dexmpm_grid_op_grad(const DexBatch *b, int epoch, const float *pose, const f
 int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *s, const float *g_next, float *g,
                     dexmpm_stream_t stream);
 
+/* One forward substep (P2G, grid update, G2P) of ONE environment that
+ * allocates no device memory: for callers that cannot call cudaMalloc, such
+ * as a host application whose own pool allocator owns the device memory, or
+ * a real-time loop that must not block on or fail in an allocation.  No
+ * counterpart in the reference.
+ *   env:    HOST pointer; p_off = blk_off = body_off = 0; grid dims multiples
+ *           of 4 with gx*gy*gz <= 262144 (64^3); n <= 1048576; n_bodies <= 32.
+ *   s, next_s: state slots of 24 planes of env->n floats (layout above).
+ *   mass, vol [n], mu_lam_yield [3][n]; body_shape, pose, next_pose [n_bodies][8].
+ *   error:  nullable device int32; DEXMPM_ERR_OUT_OF_GRID is OR-ed in when a
+ *           particle stencil leaves the grid (that particle is skipped).
+ * Grids, active-block lists and counters live in one fixed device array of
+ * this library (12.7 MB, held by every GPU that loads it until exit), shared
+ * by all calls: each call clears what must start at zero, and calls that
+ * overlap on the GPU race on it.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Returns DEXMPM_ERR_ARG for sizes beyond the limits. */
+int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *next_s, const float *mass, const float *vol,
+                           const float *mu_lam_yield, const float *body_shape, const float *pose,
+                           const float *next_pose, int32_t *error, dexmpm_stream_t stream);
+
 /* Copy out and clear the device error word (host pointer out). */
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream);
 
