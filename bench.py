@@ -172,7 +172,7 @@ def run_ours(args, rank, world, local):
     envs = build_batch(rank, args.envs)
     n_total = sum(e.n for e in envs)
     work = n_total * SUBSTEPS * ENV_STEPS  # particle-substeps per rollout
-    E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True)
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True, grid_slots=SUBSTEPS + 2)
     R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS)
     poses_h = E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs])
     R.poses.copy_(torch.from_numpy(poses_h))
@@ -183,6 +183,8 @@ def run_ours(args, rank, world, local):
     for e, env in enumerate(envs):
         counts[E.p_off[e]:E.p_off[e] + env.n] = 1.0 / env.n
     g_final = torch.zeros_like(s0)
+    from dexdeform_gb300.autotune import tune
+    tuned = tune(E, s0, R.poses[:2], use_cache=False)
 
     def loss_grad(final):
         # L = sum_e mean_p |x - target|^2 ; dL/dx = 2 (x - target) / n_e
@@ -271,8 +273,8 @@ def run_ours(args, rank, world, local):
     d2h = g0_h.numel() * 4 + bg_h.numel() * 4 + 4
 
     # ----- per-kernel timing (eager, CUDA events on the launching stream)
-    kt = kernel_times(E, R, s0, g_final)
-    roof = roofline(E, kt)
+    kt, cells = kernel_times(E, R, s0, g_final)
+    roof = roofline(E, kt, cells)
     err = E.error_word()
 
     plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
@@ -288,6 +290,7 @@ def run_ours(args, rank, world, local):
                                    "10 env steps x 50 substeps, fwd+bwd with per-env-step checkpoints, CUDA graphs",
                        "n_envs": len(envs), "particles_per_replica": n_total, "substeps": SUBSTEPS * ENV_STEPS,
                        "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
+                       "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1], "source": "autotune"},
                        "l2": "inputs larger than L2 (per-step state traffic ~4 GB >> 129 MB L2)"},
             "fwd": {"value": fwd_value, "unit": UNIT, "ms_per_step": fwd_ms / args.steps},
             "latency_ms": {"p50": ps[len(ps) // 2], "p99": ps[min(len(ps) - 1, int(math.ceil(0.99 * len(ps))) - 1)],
@@ -308,8 +311,9 @@ def run_ours(args, rank, world, local):
 
 
 def kernel_times(E, R, s0, g_final):
-    """Average device time (us) of each kernel over one env step, from CUDA
-    events around eager launches on the current stream."""
+    """Average device time (us) of each kernel over one env step (forward
+    recompute keeping its grid slots, then the adjoint), from CUDA events
+    around eager launches on the current stream."""
     import torch
     from dexdeform_gb300 import _native as N
     L, sp = E.lib, N.stream_ptr()
@@ -326,50 +330,50 @@ def kernel_times(E, R, s0, g_final):
     ring, ck = R.ring, R.ckpt
     src = ck[0]
     for s in range(T):
-        e, clear = E._next_epoch(False)
-        dst = ring[s + 1]
-        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, e, N.ptr(src), N.ptr(dst), sp), "p2g"))
-        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, e, N.ptr(R.poses[s]), N.ptr(R.poses[s + 1]), 1, sp),
-                                         "grid_op"))
-        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, e, N.ptr(src), N.ptr(dst), sp), "g2p"))
+        slot, dst = 2 + s, ring[s + 1]
+        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "p2g"))
+        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, -1, N.ptr(R.poses[s]), N.ptr(R.poses[s + 1]),
+                                                          sp), "grid_op"))
+        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
         src = dst
+    torch.cuda.synchronize()
+    cells = float(E.block_count[2:2 + T].double().mean()) * 64  # active cells per substep
     gn, g = R.gbuf[1], R.gbuf[0]
     gn.copy_(g_final)
     for s in range(T - 1, -1, -1):
-        e, clear = E._next_epoch(True)
+        slot = 2 + s
         cur = ck[0] if s == 0 else ring[s]
         nxt = ring[s + 1]
         pz, pn = R.poses[s], R.poses[s + 1]
-        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, e, N.ptr(cur), None, sp), "p2g"))
-        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, e, N.ptr(pz), N.ptr(pn), 1, sp), "grid_op"))
-        timed("g2p_grad", lambda: N.check(L.dexmpm_g2p_grad(E._bp, e, N.ptr(cur), N.ptr(nxt), N.ptr(gn), N.ptr(g), sp),
-                                          "g2p_grad"))
-        timed("grid_op_grad", lambda: N.check(L.dexmpm_grid_op_grad(E._bp, e, N.ptr(pz), N.ptr(pn), N.ptr(R.bgrad[s]),
-                                                                    N.ptr(R.bgrad[s + 1]), sp), "grid_op_grad"))
-        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, e, N.ptr(cur), N.ptr(gn), N.ptr(g), sp), "p2g_grad"))
+        timed("g2p_grad", lambda: N.check(L.dexmpm_g2p_grad(E._bp, slot, N.ptr(cur), N.ptr(nxt), N.ptr(gn), N.ptr(g),
+                                                            sp), "g2p_grad"))
+        timed("grid_op_grad", lambda: N.check(L.dexmpm_grid_op_grad(E._bp, slot, N.ptr(pz), N.ptr(pn),
+                                                                    N.ptr(R.bgrad[s]), N.ptr(R.bgrad[s + 1]), sp),
+                                              "grid_op_grad"))
+        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, slot, N.ptr(cur), N.ptr(gn), N.ptr(g), sp),
+                                          "p2g_grad"))
         gn, g = g, gn
     torch.cuda.synchronize()
-    return {k: 1e3 * sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in acc.items()}
+    return {k: 1e3 * sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in acc.items()}, cells
 
 
 # Algorithmic bytes per particle (N) and per cell of the active blocks (A)
 # for each kernel: particle state read/written once, grid float4 cells once.
 ALG_BYTES = {
     "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
-    "grid_op": (0, 48),        # (mv, m) read, v_out written, previous epoch's cells cleared
+    "grid_op": (0, 32),        # (mv, m) read, v_out written (slot kept for the adjoint)
     "g2p": (72, 16),           # x read, x v C written; v_out gathered
     "g2p_grad": (96, 32),      # x, v', dL/d(x v C)' read, dL/dx written; v_out read, dL/dv_out scattered
-    "grid_op_grad": (0, 48),   # (mv, m), dL/dv_out read, dL/d(mv, m) written
+    "grid_op_grad": (0, 80),   # (mv, m), dL/dv_out read, dL/d(mv, m) written, dL/dv_out and the slot zeroed
     "p2g_grad": (260, 16),     # x v F C + material + dL/dF', dL/dx read, dL/d(x v F C) written; dL/d(mv,m) gathered
 }
 
 
-def roofline(E, kt):
+def roofline(E, kt, cells):
     import torch
     peak, src = peaks()
     top = max(kt, key=kt.get)
     n = sum(s.n for s in E.specs)
-    cells = int(E.block_count.sum().item()) * 32  # mean active blocks of the two live epochs x 64 cells / 2
     bp, bc = ALG_BYTES[top]
     alg = bp * n + bc * cells
     achieved = alg / (kt[top] * 1e-6) / 1e9

@@ -32,11 +32,12 @@ class DexEnv(ctypes.Structure):
 
 class DexBatch(ctypes.Structure):
     _fields_ = [("n_envs", c_int32), ("n_particles", c_int32), ("n_tiles", c_int32), ("n_blocks", c_int32),
-                ("n_bodies", c_int32), ("tile_size", c_int32), ("grid_ctas", c_int32), ("reserved", c_int32),
+                ("n_bodies", c_int32), ("tile_size", c_int32), ("grid_ctas", c_int32), ("flags", c_int32),
+                ("n_slots", c_int32), ("pad0", c_int32), ("pad1", c_int32), ("pad2", c_int32),
                 ("envs", c_void_p), ("tiles", c_void_p), ("block_env", c_void_p), ("mass", c_void_p),
-                ("vol", c_void_p), ("mu_lam_yield", c_void_p), ("grid", c_void_p * 2), ("vout", c_void_p),
-                ("vout_grad", c_void_p * 2), ("in_grad", c_void_p * 2), ("block_flag", c_void_p * 2),
-                ("block_list", c_void_p * 2), ("block_count", c_void_p), ("done_counter", c_void_p),
+                ("vol", c_void_p), ("mu_lam_yield", c_void_p), ("grid", c_void_p), ("vout", c_void_p),
+                ("vout_grad", c_void_p), ("in_grad", c_void_p), ("block_flag", c_void_p),
+                ("block_list", c_void_p), ("block_count", c_void_p), ("done_counter", c_void_p),
                 ("body_shape", c_void_p), ("error", c_void_p)]
 
 
@@ -58,9 +59,9 @@ _REF_SIGS = {
 _BATCH_SIGS = {
     "dexmpm_reset": [POINTER(DexBatch), P],
     "dexmpm_p2g": [POINTER(DexBatch), c_int, P, P, P],
-    "dexmpm_grid_op": [POINTER(DexBatch), c_int, P, P, c_int, P],
+    "dexmpm_grid_op": [POINTER(DexBatch), c_int, c_int, P, P, P],
     "dexmpm_g2p": [POINTER(DexBatch), c_int, P, P, P],
-    "dexmpm_substep": [POINTER(DexBatch), c_int, P, P, P, P, c_int, P],
+    "dexmpm_substep": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P],
     "dexmpm_substep_grad": [POINTER(DexBatch), c_int, P, P, P, P, P, P, P, P, P],
     "dexmpm_g2p_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
     "dexmpm_grid_op_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],

@@ -9,9 +9,12 @@
 // by stencil base cell (a 32-wide bitonic sort on shuffles), equal keys form
 // contiguous segments, each of the 27 node contributions is summed over its
 // segment with five shuffle rounds and the segment head issues one float4
-// vector atomic (red.global.add.v4.f32).  Grids are double-buffered by epoch
-// parity; the grid update of epoch e clears what epoch e-1 touched, so there
-// is no per-substep memset.
+// vector atomic (red.global.add.v4.f32).  Grid storage is an array of slots
+// (mass/momentum grid, post-update velocities, active-block list per slot):
+// forward substeps alternate two slots and each grid update clears the slot
+// the previous substep used; the adjoint of an env step reads the slots its
+// recomputed substeps left behind and clears each one after use, so nothing
+// is recomputed in the backward and nothing is memset per substep.
 //
 // Arithmetic follows mpm/csrc/integrator.cu (kernels cited per function); the
 // SVD and stress use the cancellation-free forms of mpm_math.cuh.
@@ -23,6 +26,24 @@
 #include "../../include/dexmpm.h"
 
 using namespace dexmpm;
+
+// Compile-time tuning knobs.  Defaults were picked by timing every kernel on
+// GB300 over the 64-env batch: minimum resident CTAs per SM (register caps:
+// P2G 85, G2P adjoint 128, P2G adjoint 128 with a few spills) and a rolled
+// outer loop over the 27 stencil nodes (smaller code, fewer live registers).
+#ifndef DEX_P2G_MINB
+#define DEX_P2G_MINB 3
+#endif
+#ifndef DEX_P2G_GRAD_MINB
+#define DEX_P2G_GRAD_MINB 4
+#endif
+#ifndef DEX_G2P_GRAD_MINB
+#define DEX_G2P_GRAD_MINB 2
+#endif
+#ifndef DEX_NODE_UNROLL
+#define DEX_NODE_UNROLL 1
+#endif
+constexpr int kNodeUnroll = DEX_NODE_UNROLL;
 
 namespace {
 
@@ -47,6 +68,19 @@ __device__ __forceinline__ m33 ldm33(const float *__restrict__ S, int N, int pla
 __device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m33 &m) {
 #pragma unroll
   for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
+}
+
+__device__ __forceinline__ float *slot_grid(const DexBatch &B, int k) {
+  return B.grid + (size_t)k * B.n_blocks * 256;  // 64 cells x float4 per block
+}
+__device__ __forceinline__ float *slot_vout(const DexBatch &B, int k) {
+  return B.vout + (size_t)k * B.n_blocks * 256;
+}
+__device__ __forceinline__ uint32_t *slot_flags(const DexBatch &B, int k) {
+  return B.block_flag + (size_t)k * B.n_blocks;
+}
+__device__ __forceinline__ int32_t *slot_list(const DexBatch &B, int k) {
+  return B.block_list + (size_t)k * B.n_blocks;
 }
 
 __device__ __forceinline__ int cell_index(const DexEnv &E, int x, int y, int z) {
@@ -100,11 +134,11 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 __device__ __forceinline__ void mark_block(const DexBatch &B, int X, int blk) {
-  uint32_t *flag = B.block_flag[X] + blk;
+  uint32_t *flag = slot_flags(B, X) + blk;
   if (*reinterpret_cast<volatile uint32_t *>(flag) == 0u) {
     if (atomicExch(flag, 1u) == 0u) {
-      int slot = atomicAdd(B.block_count + X, 1);
-      B.block_list[X][slot] = blk;
+      int at = atomicAdd(B.block_count + X, 1);
+      slot_list(B, X)[at] = blk;
     }
   }
 }
@@ -161,7 +195,7 @@ __device__ __forceinline__ Lane sorted_lane(const DexBatch &B, const DexEnv &E, 
 
 // =================================================================== P2G
 // integrator.cu:84-100 (compute_svd) fused with :312-394 (p2g).
-__global__ void __launch_bounds__(256) k_p2g(DexBatch B, int X, const float *__restrict__ S,
+__global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, const float *__restrict__ S,
                                              float *__restrict__ Snext) {
   const int tile = blockIdx.x;
   const DexEnv E = B.envs[B.tiles[2 * tile]];
@@ -193,9 +227,9 @@ __global__ void __launch_bounds__(256) k_p2g(DexBatch B, int X, const float *__r
 
   Stencil st;
   make_stencil(x, E.inv_dx, st);
-  float *grid = B.grid[X];
+  float *grid = slot_grid(B, X);
 
-#pragma unroll
+#pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -230,19 +264,19 @@ __global__ void __launch_bounds__(256) k_p2g(DexBatch B, int X, const float *__r
 }
 
 // ============================================================ grid update
-// integrator.cu:647-777 on the active blocks of epoch X, then clearing of the
-// blocks of the previous epoch (Y).  The last CTA to finish resets the list
-// count of Y (ticket on done_counter; no CTA waits on another).
-__global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, const float *__restrict__ pose,
-                                                 const float *__restrict__ next_pose, int clear_grads) {
-  const int Y = X ^ 1;
+// integrator.cu:647-777 on the active blocks of slot X, then (Y >= 0) clearing
+// of the blocks slot Y used.  The last CTA to finish resets the list count of
+// Y (ticket on done_counter; no CTA waits on another).
+__global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, int Y, const float *__restrict__ pose,
+                                                 const float *__restrict__ next_pose) {
   const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
   const int per_cta = blockDim.x >> 6;
   const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
-  const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(B.grid[X]);
-  float4 *vout = reinterpret_cast<float4 *>(B.vout);
+  const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(slot_grid(B, X));
+  float4 *vout = reinterpret_cast<float4 *>(slot_vout(B, X));
+  const int32_t *list = slot_list(B, X);
   for (int item = blockIdx.x * per_cta + sub; item < cnt; item += gridDim.x * per_cta) {
-    const int blk = B.block_list[X][item];
+    const int blk = list[item];
     const DexEnv E = B.envs[B.block_env[blk]];
     const int local = blk - E.blk_off;
     const int nby = E.gy >> 2, nbz = E.gz >> 2;
@@ -268,21 +302,17 @@ __global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, const float 
     }
     vout[ci] = out;
   }
-  // clear the previous epoch's blocks
+  if (Y < 0) return;
+  // clear the blocks slot Y used
   const int cnt_y = *reinterpret_cast<volatile int *>(B.block_count + Y);
-  float4 *gy = reinterpret_cast<float4 *>(B.grid[Y]);
-  float4 *vgy = reinterpret_cast<float4 *>(B.vout_grad[Y]);
-  float4 *igy = reinterpret_cast<float4 *>(B.in_grad[Y]);
+  float4 *gy = reinterpret_cast<float4 *>(slot_grid(B, Y));
+  const int32_t *list_y = slot_list(B, Y);
+  uint32_t *flags_y = slot_flags(B, Y);
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int item = blockIdx.x * per_cta + sub; item < cnt_y; item += gridDim.x * per_cta) {
-    const int blk = B.block_list[Y][item];
-    const int ci = (blk << 6) + cell;
-    gy[ci] = z4;
-    if (clear_grads) {
-      vgy[ci] = z4;
-      igy[ci] = z4;
-    }
-    if (cell == 0) B.block_flag[Y][blk] = 0u;
+    const int blk = list_y[item];
+    gy[(blk << 6) + cell] = z4;
+    if (cell == 0) flags_y[blk] = 0u;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -298,7 +328,8 @@ __global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, const float 
 
 // =================================================================== G2P
 // integrator.cu:1059-1109.
-__global__ void __launch_bounds__(256) k_g2p(DexBatch B, const float *__restrict__ S, float *__restrict__ Snext) {
+__global__ void __launch_bounds__(256) k_g2p(DexBatch B, int X, const float *__restrict__ S,
+                                             float *__restrict__ Snext) {
   const int tile = blockIdx.x;
   const DexEnv E = B.envs[B.tiles[2 * tile]];
   const int first = B.tiles[2 * tile + 1];
@@ -310,11 +341,11 @@ __global__ void __launch_bounds__(256) k_g2p(DexBatch B, const float *__restrict
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   if (!stencil_in_grid(E, st)) return;  // reported by P2G
-  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(B.vout);
+  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   f3 nv = mk3(0.f, 0.f, 0.f);
   m33 nC = mzero();
   const float c4 = 4.f * E.inv_dx;
-#pragma unroll
+#pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -339,7 +370,7 @@ __global__ void __launch_bounds__(256) k_g2p(DexBatch B, const float *__restrict
 
 // ============================================================ G2P adjoint
 // integrator.cu:1527-1614.  Writes (not adds) the x gradient of state s.
-__global__ void __launch_bounds__(256) k_g2p_grad(DexBatch B, int X, const float *__restrict__ S,
+__global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B, int X, const float *__restrict__ S,
                                                   const float *__restrict__ Snext, const float *__restrict__ Gnext,
                                                   float *__restrict__ G) {
   const int tile = blockIdx.x;
@@ -364,10 +395,10 @@ __global__ void __launch_bounds__(256) k_g2p_grad(DexBatch B, int X, const float
   make_stencil(x, E.inv_dx, st);
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
-  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(B.vout);
-  float *vg = B.vout_grad[X];
+  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
+  float *vg = B.vout_grad;
   const float c4 = 4.f * E.inv_dx;
-#pragma unroll
+#pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -396,33 +427,41 @@ __global__ void __launch_bounds__(256) k_g2p_grad(DexBatch B, int X, const float
 }
 
 // ===================================================== grid update adjoint
-// integrator.cu:779-1057.  The per-body velocities entering each contact are
-// replayed here from (m, mv) instead of being stored by the forward.  Body-pose
-// gradients are reduced in the warp before one atomic per warp and value.
+// integrator.cu:779-1057 on the blocks of slot X.  The per-body velocities
+// entering each contact are replayed here from (m, mv) instead of being stored
+// by the forward.  Body-pose gradients are reduced in the warp before one
+// atomic per warp and value.  Every cell of a listed block gets its
+// dL/d(mv, m) written (zero where there is no mass), and dL/dv_out and the
+// slot's grid are zeroed after they are read, so the next use finds them
+// clean; the last CTA resets the slot's list.
 __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
                                                       const float *__restrict__ next_pose, float *__restrict__ bgrad,
                                                       float *__restrict__ next_bgrad) {
   const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
   const int per_cta = blockDim.x >> 6;
   const int lane = threadIdx.x & 31;
+  const bool exact_capsule = (B.flags & DEXMPM_FLAG_EXACT_CAPSULE_GRAD) != 0;
   const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
-  const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(B.grid[X]);
-  const float4 *__restrict__ vgrad = reinterpret_cast<const float4 *>(B.vout_grad[X]);
-  float4 *igrad = reinterpret_cast<float4 *>(B.in_grad[X]);
+  float4 *grid = reinterpret_cast<float4 *>(slot_grid(B, X));
+  float4 *vgrad = reinterpret_cast<float4 *>(B.vout_grad);
+  float4 *igrad = reinterpret_cast<float4 *>(B.in_grad);
+  const int32_t *list = slot_list(B, X);
+  uint32_t *flags = slot_flags(B, X);
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   // uniform trip count per CTA so that whole warps run the body loop together
   const int stride = gridDim.x * per_cta;
   const int trips = (cnt + stride - 1) / stride;
   for (int t = 0; t < trips; ++t) {
     const int item = t * stride + blockIdx.x * per_cta + sub;
     const bool in_list = item < cnt;
-    const int blk = in_list ? B.block_list[X][item] : 0;
+    const int blk = in_list ? list[item] : 0;
     const DexEnv E = B.envs[B.block_env[blk]];
     const int local = blk - E.blk_off;
     const int nby = E.gy >> 2, nbz = E.gz >> 2;
     const int bx = local / (nby * nbz), by = (local / nbz) % nby, bz = local % nbz;
     const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
     const int ci = (blk << 6) + cell;
-    const float4 g = grid[ci];
+    const float4 g = in_list ? grid[ci] : z4;
     const bool active = in_list && g.w > kMassEps;
     const float inv_m = active ? 1.f / g.w : 0.f;
     const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
@@ -445,7 +484,7 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
         }
       }
     }
-    const float4 gv4 = active ? vgrad[ci] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 gv4 = active ? vgrad[ci] : z4;
     f3 gv = boundary_backward(mk3(gv4.x, gv4.y, gv4.z), v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
     // the warp's lanes share one block, hence one env and one body count
     for (int b = nbod - 1; b >= 0; --b) {
@@ -459,7 +498,7 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
         load_pose(pose, E.body_off + b, cur);
         load_pose(next_pose, E.body_off + b, nxt);
         load_shape(B.body_shape, E.body_off + b, sh);
-        contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn, (B.reserved & DEXMPM_FLAG_EXACT_CAPSULE_GRAD) != 0);
+        contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn, exact_capsule);
       }
 #pragma unroll
       for (int c = 0; c < 7; ++c) {
@@ -472,9 +511,22 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
         }
       }
     }
-    if (active) {
+    if (in_list) {
       const f3 mom = mk3(g.x, g.y, g.z);
-      igrad[ci] = make_float4(gv.x * inv_m, gv.y * inv_m, gv.z * inv_m, -inv_m * inv_m * dot(mom, gv));
+      igrad[ci] = active ? make_float4(gv.x * inv_m, gv.y * inv_m, gv.z * inv_m, -inv_m * inv_m * dot(mom, gv)) : z4;
+      vgrad[ci] = z4;
+      grid[ci] = z4;
+      if (cell == 0) flags[blk] = 0u;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned ticket = atomicAdd(B.done_counter, 1u);
+    if (ticket == gridDim.x - 1) {
+      B.block_count[X] = 0;
+      *B.done_counter = 0u;
+      __threadfence();
     }
   }
 }
@@ -482,7 +534,7 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
 // ============================================================ P2G adjoint
 // integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad).
 // Adds to the x gradient written by k_g2p_grad and writes v, F, C gradients.
-__global__ void __launch_bounds__(128) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
+__global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
                                                   const float *__restrict__ Gnext, float *__restrict__ G,
                                                   int split) {
   const int tile = blockIdx.x / split, part = blockIdx.x % split;
@@ -512,10 +564,10 @@ __global__ void __launch_bounds__(128) k_p2g_grad(DexBatch B, int X, const float
 
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
-  const float4 *__restrict__ ig = reinterpret_cast<const float4 *>(B.in_grad[X]);
+  const float4 *__restrict__ ig = reinterpret_cast<const float4 *>(B.in_grad);
   m33 g_stress = mzero(), g_C = mzero();
   f3 g_x = mk3(0.f, 0.f, 0.f), g_v = mk3(0.f, 0.f, 0.f);
-#pragma unroll
+#pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -582,9 +634,8 @@ __global__ void __launch_bounds__(128) k_p2g_grad(DexBatch B, int X, const float
 }
 
 __global__ void k_reset_counts(DexBatch B) {
+  for (int k = threadIdx.x; k < B.n_slots; k += blockDim.x) B.block_count[k] = 0;
   if (threadIdx.x == 0) {
-    B.block_count[0] = 0;
-    B.block_count[1] = 0;
     *B.done_counter = 0u;
     *B.error = 0;
   }
@@ -593,106 +644,102 @@ __global__ void k_reset_counts(DexBatch B) {
 int check_launch() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
 
 bool valid(const DexBatch *b) {
-  return b && b->envs && b->tiles && b->block_env && b->mass && b->vol && b->mu_lam_yield && b->grid[0] &&
-         b->grid[1] && b->vout && b->block_flag[0] && b->block_flag[1] && b->block_list[0] && b->block_list[1] &&
-         b->block_count && b->done_counter && b->error && b->n_tiles >= 0 && b->n_blocks > 0 &&
-         (b->tile_size == 64 || b->tile_size == 128 || b->tile_size == 256) && b->grid_ctas > 0;
+  return b && b->envs && b->tiles && b->block_env && b->mass && b->vol && b->mu_lam_yield && b->grid && b->vout &&
+         b->block_flag && b->block_list && b->block_count && b->done_counter && b->error && b->n_tiles >= 0 &&
+         b->n_blocks > 0 && b->n_slots > 0 && (b->tile_size == 64 || b->tile_size == 128 || b->tile_size == 256) &&
+         b->grid_ctas > 0;
 }
+bool slot_ok(const DexBatch *b, int k) { return k >= 0 && k < b->n_slots; }
+bool grad_ok(const DexBatch *b) { return valid(b) && b->vout_grad && b->in_grad; }
 
 }  // namespace
 
 extern "C" {
 
-const char *dexmpm_version(void) { return "dexmpm 0.1 sm_103a"; }
+const char *dexmpm_version(void) { return "dexmpm 0.2 sm_103a"; }
 
 int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream) {
   if (!valid(b)) return DEXMPM_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t cells = (size_t)b->n_blocks * 64 * sizeof(float4);
-  for (int k = 0; k < 2; ++k) {
-    if (cudaMemsetAsync(b->grid[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
-    if (b->vout_grad[k] && cudaMemsetAsync(b->vout_grad[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
-    if (b->in_grad[k] && cudaMemsetAsync(b->in_grad[k], 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
-    if (cudaMemsetAsync(b->block_flag[k], 0, (size_t)b->n_blocks * sizeof(uint32_t), s) != cudaSuccess)
-      return DEXMPM_ERR_LAUNCH;
-  }
-  if (cudaMemsetAsync(b->vout, 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
-  k_reset_counts<<<1, 32, 0, s>>>(*b);
+  if (cudaMemsetAsync(b->grid, 0, cells * b->n_slots, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  if (cudaMemsetAsync(b->vout, 0, cells * b->n_slots, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  if (b->vout_grad && cudaMemsetAsync(b->vout_grad, 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  if (b->in_grad && cudaMemsetAsync(b->in_grad, 0, cells, s) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
+  if (cudaMemsetAsync(b->block_flag, 0, (size_t)b->n_blocks * b->n_slots * sizeof(uint32_t), s) != cudaSuccess)
+    return DEXMPM_ERR_LAUNCH;
+  k_reset_counts<<<1, 256, 0, s>>>(*b);
   return check_launch();
 }
 
-int dexmpm_p2g(const DexBatch *b, int epoch, const float *S, float *Snext, dexmpm_stream_t stream) {
-  if (!valid(b) || !S) return DEXMPM_ERR_ARG;
+int dexmpm_p2g(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm_stream_t stream) {
+  if (!valid(b) || !S || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_p2g<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Snext);
+  k_p2g<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext);
   return check_launch();
 }
 
-int dexmpm_grid_op(const DexBatch *b, int epoch, const float *pose, const float *next_pose, int clear_grads,
+int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pose, const float *next_pose,
                    dexmpm_stream_t stream) {
-  if (!valid(b) || (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape))) return DEXMPM_ERR_ARG;
-  if (clear_grads && (!b->vout_grad[0] || !b->vout_grad[1] || !b->in_grad[0] || !b->in_grad[1]))
+  if (!valid(b) || !slot_ok(b, slot) || (clear_slot >= 0 && (!slot_ok(b, clear_slot) || clear_slot == slot)))
     return DEXMPM_ERR_ARG;
-  k_grid_op<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, epoch & 1, pose, next_pose, clear_grads);
+  if (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape)) return DEXMPM_ERR_ARG;
+  k_grid_op<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, slot, clear_slot < 0 ? -1 : clear_slot, pose,
+                                                            next_pose);
   return check_launch();
 }
 
-int dexmpm_g2p(const DexBatch *b, int epoch, const float *S, float *Snext, dexmpm_stream_t stream) {
-  (void)epoch;
-  if (!valid(b) || !S || !Snext) return DEXMPM_ERR_ARG;
+int dexmpm_g2p(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm_stream_t stream) {
+  if (!valid(b) || !S || !Snext || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_g2p<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, S, Snext);
+  k_g2p<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext);
   return check_launch();
 }
 
-int dexmpm_substep(const DexBatch *b, int epoch, const float *S, float *Snext, const float *pose,
-                   const float *next_pose, int clear_grads, dexmpm_stream_t stream) {
-  int rc = dexmpm_p2g(b, epoch, S, Snext, stream);
+int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *S, float *Snext, const float *pose,
+                   const float *next_pose, dexmpm_stream_t stream) {
+  int rc = dexmpm_p2g(b, slot, S, Snext, stream);
   if (rc) return rc;
-  rc = dexmpm_grid_op(b, epoch, pose, next_pose, clear_grads, stream);
+  rc = dexmpm_grid_op(b, slot, clear_slot, pose, next_pose, stream);
   if (rc) return rc;
-  return dexmpm_g2p(b, epoch, S, Snext, stream);
+  return dexmpm_g2p(b, slot, S, Snext, stream);
 }
 
-static bool grad_ok(const DexBatch *b) {
-  return valid(b) && b->vout_grad[0] && b->vout_grad[1] && b->in_grad[0] && b->in_grad[1];
-}
-
-int dexmpm_g2p_grad(const DexBatch *b, int epoch, const float *S, const float *Snext, const float *Gnext, float *G,
+int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *S, const float *Snext, const float *Gnext, float *G,
                     dexmpm_stream_t stream) {
-  if (!grad_ok(b) || !S || !Snext || !Gnext || !G) return DEXMPM_ERR_ARG;
+  if (!grad_ok(b) || !S || !Snext || !Gnext || !G || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_g2p_grad<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Snext, Gnext, G);
+  k_g2p_grad<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext, Gnext, G);
   return check_launch();
 }
 
-int dexmpm_grid_op_grad(const DexBatch *b, int epoch, const float *pose, const float *next_pose, float *bgrad,
+int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const float *next_pose, float *bgrad,
                         float *next_bgrad, dexmpm_stream_t stream) {
-  if (!grad_ok(b)) return DEXMPM_ERR_ARG;
+  if (!grad_ok(b) || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape)) return DEXMPM_ERR_ARG;
-  k_grid_op_grad<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, epoch & 1, pose, next_pose, bgrad, next_bgrad);
+  k_grid_op_grad<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, slot, pose, next_pose, bgrad, next_bgrad);
   return check_launch();
 }
 
-int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *S, const float *Gnext, float *G,
+int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gnext, float *G,
                     dexmpm_stream_t stream) {
-  if (!grad_ok(b) || !S || !Gnext || !G) return DEXMPM_ERR_ARG;
+  if (!grad_ok(b) || !S || !Gnext || !G || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   // the adjoint is register-heavy: 128-thread CTAs, tile_size/128 of them per tile
   const int cta = b->tile_size < 128 ? b->tile_size : 128;
   const int split = b->tile_size / cta;
-  k_p2g_grad<<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, epoch & 1, S, Gnext, G, split);
+  k_p2g_grad<<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split);
   return check_launch();
 }
 
-int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *S, const float *Snext, const float *Gnext,
+int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float *Snext, const float *Gnext,
                         float *G, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
                         dexmpm_stream_t stream) {
-  int rc = dexmpm_g2p_grad(b, epoch, S, Snext, Gnext, G, stream);
+  int rc = dexmpm_g2p_grad(b, slot, S, Snext, Gnext, G, stream);
   if (rc) return rc;
-  rc = dexmpm_grid_op_grad(b, epoch, pose, next_pose, bgrad, next_bgrad, stream);
+  rc = dexmpm_grid_op_grad(b, slot, pose, next_pose, bgrad, next_bgrad, stream);
   if (rc) return rc;
-  return dexmpm_p2g_grad(b, epoch, S, Gnext, G, stream);
+  return dexmpm_p2g_grad(b, slot, S, Gnext, G, stream);
 }
 
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {

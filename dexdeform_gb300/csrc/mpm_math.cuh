@@ -354,8 +354,11 @@ DX_HD SVD3 svd3_from_deviation(const m33 &E) {
       S[j][i] = v;
     }
   o.V = meye();
+#ifndef DEX_JACOBI_SWEEPS
+#define DEX_JACOBI_SWEEPS 4
+#endif
 #pragma unroll 1
-  for (int sweep = 0; sweep < 5; ++sweep) {
+  for (int sweep = 0; sweep < DEX_JACOBI_SWEEPS; ++sweep) {
     jacobi_rotate(S, o.V, 0, 1, 2);
     jacobi_rotate(S, o.V, 0, 2, 1);
     jacobi_rotate(S, o.V, 1, 2, 0);

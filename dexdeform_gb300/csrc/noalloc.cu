@@ -10,7 +10,7 @@
 // needs live in one file-scope device array of fixed size, below.
 //
 // Limits of that array: grids up to 262,144 cells (64^3, the reference's
-// default domain) and up to 1,048,576 particles, 32 bodies.  It takes 12.7 MB
+// default domain) and up to 1,048,576 particles, 32 bodies.  It takes 8.5 MB
 // on every GPU that loads this part of the library, held until the process
 // exits (with CUDA's default lazy module loading that happens on the first
 // call on a device).
@@ -36,16 +36,13 @@ constexpr int kMaxTiles = kMaxParticles / kTile;
 
 // byte offsets inside the array (each region 256-byte aligned)
 constexpr size_t kGrid0 = 0;
-constexpr size_t kGrid1 = kGrid0 + (size_t)kMaxCells * 16;
-constexpr size_t kVout = kGrid1 + (size_t)kMaxCells * 16;
+constexpr size_t kVout = kGrid0 + (size_t)kMaxCells * 16;
 constexpr size_t kFlag0 = kVout + (size_t)kMaxCells * 16;
-constexpr size_t kFlag1 = kFlag0 + (size_t)kMaxBlocks * 4;
-constexpr size_t kList0 = kFlag1 + (size_t)kMaxBlocks * 4;
-constexpr size_t kList1 = kList0 + (size_t)kMaxBlocks * 4;
-constexpr size_t kBlockEnv = kList1 + (size_t)kMaxBlocks * 4;
+constexpr size_t kList0 = kFlag0 + (size_t)kMaxBlocks * 4;
+constexpr size_t kBlockEnv = kList0 + (size_t)kMaxBlocks * 4;
 constexpr size_t kTiles = kBlockEnv + (size_t)kMaxBlocks * 4;
 constexpr size_t kEnv = kTiles + (size_t)kMaxTiles * 8;
-constexpr size_t kCounts = kEnv + 256;  // block_count[2], done_counter, error
+constexpr size_t kCounts = kEnv + 256;  // block_count, done_counter, error
 constexpr size_t kBytes = kCounts + 256;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
@@ -76,7 +73,6 @@ __global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks, int32_t *
   int32_t *tiles = reinterpret_cast<int32_t *>(base + kTiles);
   int32_t *block_env = reinterpret_cast<int32_t *>(base + kBlockEnv);
   uint32_t *flag0 = reinterpret_cast<uint32_t *>(base + kFlag0);
-  uint32_t *flag1 = reinterpret_cast<uint32_t *>(base + kFlag1);
   int stride = gridDim.x * blockDim.x;
   int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   for (int t = t0; t < n_tiles; t += stride) {
@@ -86,13 +82,11 @@ __global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks, int32_t *
   for (int b = t0; b < n_blocks; b += stride) {
     block_env[b] = 0;
     flag0[b] = 0u;
-    flag1[b] = 0u;
   }
   if (t0 == 0) {
     *reinterpret_cast<DexEnv *>(base + kEnv) = env;
     int32_t *counts = reinterpret_cast<int32_t *>(base + kCounts);
-    counts[0] = 0;
-    counts[1] = 0;
+    counts[0] = 0;  // block count of the single slot
     counts[2] = 0;  // done_counter
     if (caller_error == nullptr) counts[3] = 0;
   }
@@ -133,26 +127,25 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   b.n_bodies = e.n_bodies;
   b.tile_size = kTile;
   b.grid_ctas = 152 * 4;
-  b.reserved = 0;
+  b.flags = 0;
+  b.n_slots = 1;
+  b.pad0 = b.pad1 = b.pad2 = 0;
   b.envs = reinterpret_cast<const DexEnv *>(base + kEnv);
   b.tiles = reinterpret_cast<const int32_t *>(base + kTiles);
   b.block_env = reinterpret_cast<const int32_t *>(base + kBlockEnv);
   b.mass = mass;
   b.vol = vol;
   b.mu_lam_yield = mu_lam_yield;
-  b.grid[0] = reinterpret_cast<float *>(base + kGrid0);
-  b.grid[1] = reinterpret_cast<float *>(base + kGrid1);
+  b.grid = reinterpret_cast<float *>(base + kGrid0);
   b.vout = reinterpret_cast<float *>(base + kVout);
-  b.vout_grad[0] = b.vout_grad[1] = nullptr;
-  b.in_grad[0] = b.in_grad[1] = nullptr;
-  b.block_flag[0] = reinterpret_cast<uint32_t *>(base + kFlag0);
-  b.block_flag[1] = reinterpret_cast<uint32_t *>(base + kFlag1);
-  b.block_list[0] = reinterpret_cast<int32_t *>(base + kList0);
-  b.block_list[1] = reinterpret_cast<int32_t *>(base + kList1);
+  b.vout_grad = nullptr;
+  b.in_grad = nullptr;
+  b.block_flag = reinterpret_cast<uint32_t *>(base + kFlag0);
+  b.block_list = reinterpret_cast<int32_t *>(base + kList0);
   b.block_count = reinterpret_cast<int32_t *>(base + kCounts);
   b.done_counter = reinterpret_cast<uint32_t *>(base + kCounts + 8);
   b.body_shape = body_shape;
   b.error = error ? error : reinterpret_cast<int32_t *>(base + kCounts + 12);
-  // epoch 0: P2G into grid 0; the grid update finds list 1 empty
-  return dexmpm_substep(&b, 0, s, next_s, pose, next_pose, 0, stream);
+  // one grid slot, nothing to clear afterwards (the next call re-zeroes it)
+  return dexmpm_substep(&b, 0, -1, s, next_s, pose, next_pose, stream);
 }

@@ -1,9 +1,12 @@
-"""Batched MLS-MPM engine: device buffers, epochs and checkpointed rollouts.
+"""Batched MLS-MPM engine: device buffers, grid slots and checkpointed rollouts.
 
 A ``BatchEngine`` owns the device memory of a batch of environments (particle
-state slots in SoA planes, block-sparse grids, active-block lists, body shapes)
-and launches the kernels of libdexmpm.so through its C ABI.  A ``Rollout``
-runs env steps of ``T`` substeps forward with one checkpoint per env step and
+state slots in SoA planes, grid slots with active-block lists, body shapes)
+and launches the kernels of libdexmpm.so through its C ABI.  Forward
+substeps alternate grid slots 0 and 1; an engine built with more slots lets a
+recomputed env step keep one grid slot per substep, which its adjoint then
+reads instead of recomputing P2G and the grid update.  A ``Rollout`` runs env
+steps of ``T`` substeps forward with one checkpoint per env step and
 back-propagates by recomputing each env step's substeps from its checkpoint,
 each env step captured once as a CUDA graph and replayed.
 
@@ -63,12 +66,15 @@ def pack_poses(pos: np.ndarray, rot: np.ndarray) -> np.ndarray:
 
 def footprint_bytes(specs: Sequence[EnvSpec], n_slots: int = 2, grad: bool = False, substeps: int = 0,
                     env_steps: int = 0) -> int:
-    """Device bytes a batch needs (used by admission control)."""
+    """Device bytes a batch needs (used by admission control): grid slots
+    (2, plus one per substep of an env step with gradients), state slots,
+    checkpoints and poses."""
     n = sum(s.n for s in specs)
     blocks = sum((s.grid_dim[0] // 4) * (s.grid_dim[1] // 4) * (s.grid_dim[2] // 4) for s in specs)
     nb = sum(s.nb for s in specs)
-    grid_bufs = 3 + (4 if grad else 0)
-    b = blocks * 64 * 16 * grid_bufs + blocks * 4 * 5
+    grid_slots = 2 + (substeps if grad else 0)
+    b = blocks * 64 * 32 * grid_slots + blocks * 8 * grid_slots + blocks * 4
+    b += blocks * 64 * 32 if grad else 0
     slots = n_slots + ((env_steps + 1) + (substeps + 1) + 2 if grad else 0)
     b += slots * 24 * 4 * n + 5 * 4 * n
     b += (env_steps * substeps + 1) * nb * 32 * (2 if grad else 1)
@@ -106,8 +112,10 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
 class BatchEngine:
     def __init__(self, specs: Sequence[EnvSpec], device="cuda", tile_size: int = 128,
                  grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False,
-                 capsule_grad: str = "reference"):
-        """capsule_grad: "reference" drops the capsule-normal term of the body
+                 capsule_grad: str = "reference", grid_slots: int = 2):
+        """grid_slots: 2 for forward use; 2 + T lets Rollout / DiffSim keep the
+        grids of a recomputed env step of T substeps for the adjoint.
+        capsule_grad: "reference" drops the capsule-normal term of the body
         pose gradient as the reference does; "exact" keeps it."""
         N.require_cuda()
         self.lib = N.load()
@@ -151,37 +159,35 @@ class BatchEngine:
         self.mly = torch.tensor(mly, **f32)
         self.body_shape = torch.tensor(shapes, **f32)
         cells = self.n_blocks * 64
-        self.grid = [torch.zeros((cells, 4), **f32) for _ in range(2)]
-        self.vout = torch.zeros((cells, 4), **f32)
-        self.vout_grad = [torch.zeros((cells, 4), **f32) for _ in range(2)] if grad else [None, None]
-        self.in_grad = [torch.zeros((cells, 4), **f32) for _ in range(2)] if grad else [None, None]
-        self.block_flag = [torch.zeros(self.n_blocks, **i32) for _ in range(2)]
-        self.block_list = [torch.zeros(self.n_blocks, **i32) for _ in range(2)]
-        self.block_count = torch.zeros(2, **i32)
+        self.n_grid_slots = K = max(2, int(grid_slots))
+        self.grid = torch.zeros((K, cells, 4), **f32)
+        self.vout = torch.zeros((K, cells, 4), **f32)
+        self.vout_grad = torch.zeros((cells, 4), **f32) if grad else None
+        self.in_grad = torch.zeros((cells, 4), **f32) if grad else None
+        self.block_flag = torch.zeros((K, self.n_blocks), **i32)
+        self.block_list = torch.zeros((K, self.n_blocks), **i32)
+        self.block_count = torch.zeros(K, **i32)
         self.done_counter = torch.zeros(1, **i32)
         self.error = torch.zeros(1, **i32)
         self.states = torch.zeros((n_slots, N.STATE_PLANES, Np), **f32)
-        self.grid_ctas = int(grid_ctas or SM_COUNT * 8)
+        self.grid_ctas = int(grid_ctas or SM_COUNT * 4)
         b = N.DexBatch()
         b.n_envs, b.n_particles, b.n_tiles, b.n_blocks = len(self.specs), Np, len(tiles), self.n_blocks
         b.n_bodies, b.tile_size, b.grid_ctas = self.n_bodies, self.tile_size, self.grid_ctas
         assert capsule_grad in ("reference", "exact")
-        b.reserved = N.FLAG_EXACT_CAPSULE_GRAD if capsule_grad == "exact" else 0
+        b.flags = N.FLAG_EXACT_CAPSULE_GRAD if capsule_grad == "exact" else 0
+        b.n_slots = K
         b.envs, b.tiles, b.block_env = self.envs_t.data_ptr(), self.tiles_t.data_ptr(), self.block_env_t.data_ptr()
         b.mass, b.vol, b.mu_lam_yield = self.mass.data_ptr(), self.vol.data_ptr(), self.mly.data_ptr()
-        for k in range(2):
-            b.grid[k] = self.grid[k].data_ptr()
-            b.vout_grad[k] = self.vout_grad[k].data_ptr() if grad else None
-            b.in_grad[k] = self.in_grad[k].data_ptr() if grad else None
-            b.block_flag[k] = self.block_flag[k].data_ptr()
-            b.block_list[k] = self.block_list[k].data_ptr()
-        b.vout = self.vout.data_ptr()
+        b.grid, b.vout = self.grid.data_ptr(), self.vout.data_ptr()
+        b.vout_grad = self.vout_grad.data_ptr() if grad else None
+        b.in_grad = self.in_grad.data_ptr() if grad else None
+        b.block_flag, b.block_list = self.block_flag.data_ptr(), self.block_list.data_ptr()
         b.block_count, b.done_counter = self.block_count.data_ptr(), self.done_counter.data_ptr()
         b.body_shape, b.error = self.body_shape.data_ptr(), self.error.data_ptr()
         self.batch = b
         self._bp = ctypes.byref(b)
-        self.epoch = 0
-        self.prev_backward = False
+        self.fslot = 0          # grid slot of the next forward substep (0 or 1)
         self.launches = 0
         N.check(self.lib.dexmpm_reset(self._bp, N.stream_ptr()), "dexmpm_reset")
 
@@ -221,52 +227,74 @@ class BatchEngine:
         return out
 
     # ------------------------------------------------------------ kernels
-    def _next_epoch(self, backward: bool):
-        e = self.epoch
-        clear = 1 if (self.prev_backward or backward) and self.grad else 0
-        self.epoch += 1
-        self.prev_backward = backward
-        return e, clear
-
     def substep(self, s: torch.Tensor, s_next: torch.Tensor, pose: torch.Tensor, next_pose: torch.Tensor,
-                force_clear: bool = False):
-        """One forward substep (P2G, grid update, G2P) of every env."""
-        e, clear = self._next_epoch(False)
-        if force_clear and self.grad:
-            clear = 1
-        N.check(self.lib.dexmpm_substep(self._bp, e, N.ptr(s), N.ptr(s_next), N.ptr(pose), N.ptr(next_pose),
-                                        clear, N.stream_ptr()), "dexmpm_substep")
+                slot: Optional[int] = None):
+        """One forward substep (P2G, grid update, G2P) of every env.  Without
+        `slot` it uses the forward slot pair (alternating, each clearing the
+        other); with `slot` (>= 2) it fills that grid slot and keeps it for the
+        adjoint of this substep."""
+        if slot is None:
+            slot, clear = self.fslot, self.fslot ^ 1
+            self.fslot ^= 1
+        else:
+            assert 2 <= slot < self.n_grid_slots
+            clear = -1
+        N.check(self.lib.dexmpm_substep(self._bp, slot, clear, N.ptr(s), N.ptr(s_next), N.ptr(pose),
+                                        N.ptr(next_pose), N.stream_ptr()), "dexmpm_substep")
         self.launches += 3
+        return slot
 
-    def substep_grad(self, s, s_next, g_next, g, pose, next_pose, bgrad, next_bgrad, force_clear: bool = False):
-        """Adjoint of one substep: recompute P2G and grid update from s, then
-        G2P, grid and P2G adjoints.  g (gradient of s) is overwritten."""
+    def substep_grad(self, s, s_next, g_next, g, pose, next_pose, bgrad, next_bgrad, slot: Optional[int] = None):
+        """Adjoint of one substep: G2P, grid and P2G adjoints.  With `slot` the
+        grid slot left by that substep's forward is used (and cleared);
+        without, P2G and the grid update are recomputed from s first.
+        g (gradient of s) is overwritten."""
         assert self.grad, "engine built without gradient buffers"
-        e, clear = self._next_epoch(True)
-        if force_clear:
-            clear = 1
         sp = N.stream_ptr()
-        N.check(self.lib.dexmpm_p2g(self._bp, e, N.ptr(s), None, sp), "dexmpm_p2g")
-        N.check(self.lib.dexmpm_grid_op(self._bp, e, N.ptr(pose), N.ptr(next_pose), clear, sp), "dexmpm_grid_op")
-        N.check(self.lib.dexmpm_substep_grad(self._bp, e, N.ptr(s), N.ptr(s_next), N.ptr(g_next), N.ptr(g),
+        if slot is None:
+            slot, clear = self.fslot, self.fslot ^ 1
+            self.fslot ^= 1
+            N.check(self.lib.dexmpm_p2g(self._bp, slot, N.ptr(s), None, sp), "dexmpm_p2g")
+            N.check(self.lib.dexmpm_grid_op(self._bp, slot, clear, N.ptr(pose), N.ptr(next_pose), sp),
+                    "dexmpm_grid_op")
+            self.launches += 2
+        N.check(self.lib.dexmpm_substep_grad(self._bp, slot, N.ptr(s), N.ptr(s_next), N.ptr(g_next), N.ptr(g),
                                              N.ptr(pose), N.ptr(next_pose), N.ptr(bgrad), N.ptr(next_bgrad), sp),
                 "dexmpm_substep_grad")
-        self.launches += 5
+        self.launches += 3
+
+    def retune(self, tile_size: int, grid_ctas: int):
+        """Change the particle tile size and the persistent grid-kernel CTA
+        count (launch shape only; no buffer changes)."""
+        assert tile_size in (64, 128, 256) and grid_ctas > 0
+        L = plan_layout(self.specs, tile_size)
+        tiles = L["tiles"]
+        self.tile_size, self.grid_ctas = int(tile_size), int(grid_ctas)
+        self.tiles_t = torch.tensor(np.asarray(tiles, np.int32).reshape(-1, 2) if tiles else
+                                    np.zeros((0, 2), np.int32), dtype=torch.int32, device=self.device)
+        b = self.batch
+        b.tiles, b.n_tiles, b.tile_size, b.grid_ctas = self.tiles_t.data_ptr(), len(tiles), self.tile_size, \
+            self.grid_ctas
 
     def error_word(self) -> int:
         out = ctypes.c_int32(0)
         N.check(self.lib.dexmpm_get_error(self._bp, ctypes.byref(out), N.stream_ptr()), "dexmpm_get_error")
         return int(out.value)
 
-    def active_blocks(self, epoch_parity: int) -> int:
-        return int(self.block_count[epoch_parity].item())
+    def active_blocks(self, slot: int) -> int:
+        return int(self.block_count[slot].item())
+
+    def grid_mass(self, slot: int) -> float:
+        return float(self.grid[slot, :, 3].double().sum())
 
 
 class Rollout:
     """Env steps of T substeps over a BatchEngine, with per-env-step
     checkpoints (grad mode) and substep recomputation in the backward pass.
-    Each env step's forward and backward are captured as CUDA graphs on first
-    use and replayed afterwards."""
+    When the engine has T + 2 grid slots, the recomputed substeps keep their
+    grids and the adjoint reads them; otherwise the adjoint recomputes P2G and
+    the grid update per substep.  Each env step's forward and backward are
+    captured as CUDA graphs on first use and replayed afterwards."""
 
     def __init__(self, engine: BatchEngine, substeps: int, env_steps: int, use_graphs: bool = True):
         self.E = engine
@@ -275,6 +303,7 @@ class Rollout:
         dev = engine.device
         nb = max(engine.n_bodies, 1)
         self.poses = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
+        self.keep_grids = engine.n_grid_slots >= self.T + 2
         if engine.grad:
             self.ckpt = engine.new_slots(self.S + 1)
             self.ring = engine.new_slots(self.T + 1)
@@ -296,7 +325,7 @@ class Rollout:
         for s in range(T):
             t = k * T + s
             dst = self._ckpt(k + 1) if s == T - 1 else self.ring[s % 2]
-            E.substep(src, dst, self.poses[t], self.poses[t + 1], force_clear=(s == 0))
+            E.substep(src, dst, self.poses[t], self.poses[t + 1])
             src = dst
 
     def forward_step(self, k: int):
@@ -312,20 +341,22 @@ class Rollout:
     # ------------------------------------------------------------ backward
     def _backward_step(self, k: int):
         """Gradient of ckpt[k] from the gradient of ckpt[k+1] (in gbuf[1]):
-        recompute the T states of env step k into the ring, then run the
-        adjoint substeps in reverse.  Result in gbuf[1]."""
+        recompute the T states of env step k into the ring (keeping each
+        substep's grid slot when there are enough slots), then run the adjoint
+        substeps in reverse.  Result in gbuf[1]."""
         T, E = self.T, self.E
         src = self.ckpt[k]
         for s in range(T):
             t = k * T + s
-            E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1], force_clear=(s == 0))
+            E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1],
+                      slot=(2 + s) if self.keep_grids else None)
             src = self.ring[s + 1]
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):
             t = k * T + s
             cur = self.ckpt[k] if s == 0 else self.ring[s]
             E.substep_grad(cur, self.ring[s + 1], g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
-                           self.bgrad[t + 1])
+                           self.bgrad[t + 1], slot=(2 + s) if self.keep_grids else None)
             g_next, g = g, g_next
         if T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])
@@ -348,35 +379,36 @@ class Rollout:
 
     # -------------------------------------------------------------- graphs
     def _run(self, cache, k, fn):
-        if not self.use_graphs:
-            fn(k)
-            return
-        E = self.E
-        g = cache.get((k, E.epoch & 1))
-        if g is None:
-            # run eagerly once (this is the call's work), then capture at the
-            # epoch parity reached, which is the parity of later calls when
-            # the step spans an even number of epochs
-            fn(k)
-            torch.cuda.synchronize()
-            key = (k, E.epoch & 1)
-            g = torch.cuda.CUDAGraph()
-            s = torch.cuda.Stream()
-            s.wait_stream(torch.cuda.current_stream())
-            epoch0, prev0, launches0 = E.epoch, E.prev_backward, E.launches
-            with torch.cuda.stream(s):
-                g.capture_begin()
-                fn(k)
-                g.capture_end()
-            torch.cuda.current_stream().wait_stream(s)
-            self._graph_epochs = E.epoch - epoch0
-            E.epoch, E.prev_backward, E.launches = epoch0, prev0, launches0
-            cache[key] = g
-            # the warm-up call already advanced the state by one step; the
-            # capture did not execute, so this call is done
-            return
-        g.replay()
-        steps = self.T if cache is self._fwd_graphs else 2 * self.T
-        E.epoch += steps
-        E.prev_backward = cache is self._bwd_graphs
-        E.launches += 3 * self.T if cache is self._fwd_graphs else 8 * self.T
+        run_graph(self.E, cache, k, lambda: fn(k), self.use_graphs)
+
+
+def run_graph(E: BatchEngine, cache: dict, key, fn, use_graphs: bool = True):
+    """Run fn (a fixed launch sequence) through a CUDA graph cached under
+    (key, forward slot parity).  The first call runs fn eagerly -- that is
+    the call's work -- and captures it; later calls replay it.  The host-side
+    slot parity and launch counter advance as the eager run advanced them."""
+    if not use_graphs:
+        fn()
+        return
+    entry = cache.get((key, E.fslot))
+    if entry is None:
+        f0, l0 = E.fslot, E.launches
+        fn()
+        torch.cuda.synchronize()
+        df, dl = E.fslot ^ f0, E.launches - l0
+        f1 = E.fslot
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            g.capture_begin()
+            fn()
+            g.capture_end()
+        torch.cuda.current_stream().wait_stream(side)
+        E.fslot, E.launches = f1, l0 + dl
+        cache[(key, f1)] = (g, df, dl)
+        return
+    g, df, dl = entry
+    g.replay()
+    E.fslot ^= df
+    E.launches += dl

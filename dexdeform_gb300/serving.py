@@ -31,7 +31,7 @@ from typing import Dict, List, Optional
 import numpy as np
 import torch
 
-from .engine import BatchEngine, EnvSpec, footprint_bytes, pack_poses
+from .engine import BatchEngine, EnvSpec, footprint_bytes, pack_poses, run_graph
 
 
 @dataclass
@@ -81,7 +81,8 @@ class _Batch:
 
     def __init__(self, reqs: List[Request], substeps: int, grad: bool, device, tile_size: int, use_graphs: bool):
         self.ids = tuple(r.rid for r in reqs)
-        self.E = BatchEngine([r.spec for r in reqs], device=device, grad=grad, tile_size=tile_size)
+        self.E = BatchEngine([r.spec for r in reqs], device=device, grad=grad, tile_size=tile_size,
+                             grid_slots=substeps + 2 if grad else 2)
         self.T = substeps
         nb = max(self.E.n_bodies, 1)
         self.slot = self.E.new_slots(self.T + 1)
@@ -94,45 +95,22 @@ class _Batch:
 
     def _forward(self):
         for s in range(self.T):
-            self.E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], force_clear=(s == 0))
+            self.E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1])
 
     def _backward(self):
-        self._forward()
         E = self.E
+        for s in range(self.T):
+            E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s)
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.slot[s], self.slot[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1])
+                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s)
             g_next, g = g, g_next
         if self.T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])
 
     def run(self, kind: str):
-        fn = self._forward if kind == "fwd" else self._backward
-        E = self.E
-        if not self.use_graphs:
-            fn()
-            return
-        key = (kind, E.epoch & 1)
-        g = self.graphs.get(key)
-        if g is None:
-            fn()
-            e0, p0, l0 = E.epoch, E.prev_backward, E.launches
-            g = torch.cuda.CUDAGraph()
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(side):
-                g.capture_begin()
-                fn()
-                g.capture_end()
-            torch.cuda.current_stream().wait_stream(side)
-            E.epoch, E.prev_backward, E.launches = e0, p0, l0
-            self.graphs[(kind, E.epoch & 1)] = g
-            return
-        g.replay()
-        E.epoch += self.T if kind == "fwd" else 2 * self.T
-        E.prev_backward = kind == "bwd"
-        E.launches += 3 * self.T if kind == "fwd" else 8 * self.T
+        run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward, self.use_graphs)
 
 
 class Server:

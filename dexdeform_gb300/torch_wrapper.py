@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .engine import BatchEngine, EnvSpec
+from .engine import BatchEngine, EnvSpec, run_graph
 
 
 def pack_pose_tensor(pos: torch.Tensor, rot: torch.Tensor) -> torch.Tensor:
@@ -31,12 +31,16 @@ def pack_pose_tensor(pos: torch.Tensor, rot: torch.Tensor) -> torch.Tensor:
 
 
 class DiffSim:
-    """Differentiable batched simulator core: T substeps per env step."""
+    """Differentiable batched simulator core: T substeps per env step.  The
+    adjoint recomputes the env step from its input state into a ring of T+1
+    state slots, keeping each substep's grid slot, then runs the adjoint
+    kernels in reverse on those slots."""
 
     def __init__(self, specs: Sequence[EnvSpec], substeps: int, device="cuda", tile_size=128, use_graphs=True,
                  capsule_grad="reference"):
-        self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size, capsule_grad=capsule_grad)
         self.T = int(substeps)
+        self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size, capsule_grad=capsule_grad,
+                             grid_slots=self.T + 2)
         self.nb = max(self.E.n_bodies, 1)
         self.ring = self.E.new_slots(self.T + 1)
         self.gbuf = self.E.new_slots(2)
@@ -50,50 +54,24 @@ class DiffSim:
     def _fwd(self):
         E = self.E
         for s in range(self.T):
-            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], force_clear=(s == 0))
+            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1])
 
     def _bwd(self):
         E = self.E
-        self._fwd()
+        for s in range(self.T):
+            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s)
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.ring[s], self.ring[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1])
+                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s)
             g_next, g = g, g_next
         if self.T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])
 
-    def _replay(self, name, fn, epochs):
-        E = self.E
-        if not self.use_graphs:
-            fn()
-            return
-        key = (name, E.epoch & 1)
-        g = self._g.get(key)
-        if g is None:
-            fn()
-            torch.cuda.synchronize()
-            e0, p0, l0 = E.epoch, E.prev_backward, E.launches
-            g = torch.cuda.CUDAGraph()
-            s = torch.cuda.Stream()
-            s.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(s):
-                g.capture_begin()
-                fn()
-                g.capture_end()
-            torch.cuda.current_stream().wait_stream(s)
-            E.epoch, E.prev_backward, E.launches = e0, p0, l0
-            self._g[(name, E.epoch & 1)] = g
-            return
-        g.replay()
-        E.epoch += epochs
-        E.prev_backward = name == "bwd"
-        E.launches += 3 * self.T if name == "fwd" else 8 * self.T
-
     def forward(self, state: torch.Tensor, poses: torch.Tensor) -> torch.Tensor:
         self.ring[0].copy_(state)
         self.poses.copy_(poses)
-        self._replay("fwd", self._fwd, self.T)
+        run_graph(self.E, self._g, "fwd", self._fwd, self.use_graphs)
         return self.ring[self.T].clone()
 
     def backward(self, state: torch.Tensor, poses: torch.Tensor, g_out: torch.Tensor):
@@ -101,7 +79,7 @@ class DiffSim:
         self.poses.copy_(poses)
         self.gbuf[1].copy_(g_out)
         self.bgrad.zero_()
-        self._replay("bwd", self._bwd, 2 * self.T)
+        run_graph(self.E, self._g, "bwd", self._bwd, self.use_graphs)
         return self.gbuf[1].clone(), self.bgrad.clone()
 
 

@@ -127,12 +127,19 @@ int dexmpm_abi_get_error(int32_t *out);
  * Grids: every env owns gx*gy*gz cells (dims multiples of 4) stored as 4^3
  *   blocks; block b of the whole batch holds cells [64b, 64b+64), cell
  *   (x,y,z) of env e is block blk_off + ((x>>2)*(gy/4) + (y>>2))*(gz/4) + (z>>2),
- *   slot ((x&3)*16 + (y&3)*4 + (z&3)).  Cell values are float4:
- *     grid[k]      (m v.x, m v.y, m v.z, m) after P2G
- *     vout         (v.x, v.y, v.z, 0) after the grid update
- *     vout_grad[k] dL/dv_out, in_grad[k] (dL/d(mv), dL/dm)
- *   k = epoch & 1: each P2G starts an epoch; the grid update of epoch e
- *   clears the blocks epoch e-1 used, so no per-substep memset is needed.
+ *   slot ((x&3)*16 + (y&3)*4 + (z&3)).  Cell values are float4.
+ * Grid slots: `n_slots` copies of
+ *     grid   (m v.x, m v.y, m v.z, m) after P2G
+ *     vout   (v.x, v.y, v.z, m) after the grid update
+ *   with a block flag array, an active-block list and its count per slot.
+ *   P2G into slot k appends the blocks its stencils touch to slot k's list.
+ *   Forward substeps alternate two slots; each grid update clears the slot of
+ *   the previous substep (clear_slot).  The adjoint of a substep reads the
+ *   slot its forward left behind and clears it, so recomputed substeps can
+ *   keep one slot each until their adjoint runs.  No per-substep memset.
+ * Gradient grids (one each): vout_grad dL/dv_out, in_grad (dL/d(mv), dL/dm);
+ *   the grid adjoint zeroes vout_grad after reading it and writes in_grad for
+ *   every cell of its blocks.
  * Poses: [n_bodies][8] floats per substep boundary: p.x p.y p.z 0 q.w q.x q.y q.z.
  * Body shapes: [n_bodies][8]: type friction softness round, args w x y z.
  * Body-pose gradients: [n_bodies][8] in the pose layout, accumulated.
@@ -151,65 +158,65 @@ typedef struct {
 
 typedef struct {
   int32_t n_envs, n_particles, n_tiles, n_blocks;
-  int32_t n_bodies, tile_size, grid_ctas, reserved; /* reserved = flags (DEXMPM_FLAG_*) */
+  int32_t n_bodies, tile_size, grid_ctas, flags; /* flags: DEXMPM_FLAG_* */
+  int32_t n_slots, pad0, pad1, pad2;
   const DexEnv *envs;         /* [n_envs] */
   const int32_t *tiles;       /* [n_tiles][2]: env, first particle within the env */
   const int32_t *block_env;   /* [n_blocks]: owning env */
   const float *mass;          /* [n_particles] */
   const float *vol;           /* [n_particles] */
   const float *mu_lam_yield;  /* [3][n_particles] */
-  float *grid[2];             /* [n_blocks*64] float4 */
-  float *vout;                /* [n_blocks*64] float4 */
-  float *vout_grad[2];        /* [n_blocks*64] float4 */
-  float *in_grad[2];          /* [n_blocks*64] float4 */
-  uint32_t *block_flag[2];    /* [n_blocks] */
-  int32_t *block_list[2];     /* [n_blocks] */
-  int32_t *block_count;       /* [2] */
+  float *grid;                /* [n_slots][n_blocks*64] float4 */
+  float *vout;                /* [n_slots][n_blocks*64] float4 */
+  float *vout_grad;           /* [n_blocks*64] float4, nullable without gradients */
+  float *in_grad;             /* [n_blocks*64] float4, nullable without gradients */
+  uint32_t *block_flag;       /* [n_slots][n_blocks] */
+  int32_t *block_list;        /* [n_slots][n_blocks] */
+  int32_t *block_count;       /* [n_slots] */
   uint32_t *done_counter;     /* [1] */
   const float *body_shape;    /* [n_bodies][8] */
   int32_t *error;             /* [1] sticky DEXMPM_ERR_* bits */
 } DexBatch;
 
-/* Zero every grid buffer, flag, list count and the error word.  Call once after
- * allocation (and after any fault) -- the epochs keep them clean afterwards. */
+/* Zero every grid slot, flag, list count and the error word.  Call once after
+ * allocation -- the slot protocol keeps them clean afterwards. */
 int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream);
 
-/* P2G of epoch `epoch`: SVD, von Mises, stress, APIC scatter of state slot s
- * into grid[epoch&1]; appends the touched blocks to block_list[epoch&1].
- * F_out (nullable) receives the projected F (9 planes at the F offset of the
- * next state slot). */
-int dexmpm_p2g(const DexBatch *b, int epoch, const float *s, float *next_s, dexmpm_stream_t stream);
+/* P2G into grid slot `slot`: SVD, von Mises, stress, APIC scatter of state
+ * slot s; appends the touched blocks to the slot's list.  next_s (nullable)
+ * receives the projected F (its 9 F planes). */
+int dexmpm_p2g(const DexBatch *b, int slot, const float *s, float *next_s, dexmpm_stream_t stream);
 
-/* Grid update of epoch `epoch` on its active blocks, with body poses at the
- * substep start (pose) and end (next_pose); clears the blocks of epoch-1
- * (their gradient buffers too when clear_grads != 0). */
-int dexmpm_grid_op(const DexBatch *b, int epoch, const float *pose, const float *next_pose, int clear_grads,
+/* Grid update on the active blocks of `slot`, with body poses at the substep
+ * start (pose) and end (next_pose); then clears grid slot clear_slot (< 0: none). */
+int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pose, const float *next_pose,
                    dexmpm_stream_t stream);
 
-/* G2P of epoch `epoch`: x, v, C of next_s from s and vout. */
-int dexmpm_g2p(const DexBatch *b, int epoch, const float *s, float *next_s, dexmpm_stream_t stream);
+/* G2P from grid slot `slot`: x, v, C of next_s from s. */
+int dexmpm_g2p(const DexBatch *b, int slot, const float *s, float *next_s, dexmpm_stream_t stream);
 
 /* One forward substep: dexmpm_p2g + dexmpm_grid_op + dexmpm_g2p. */
-int dexmpm_substep(const DexBatch *b, int epoch, const float *s, float *next_s, const float *pose,
-                   const float *next_pose, int clear_grads, dexmpm_stream_t stream);
+int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *s, float *next_s, const float *pose,
+                   const float *next_pose, dexmpm_stream_t stream);
 
-/* Adjoint of one substep whose forward (p2g + grid_op) was just recomputed in
- * epoch `epoch` from state slot s.  next_s is the state after the substep (its
- * v sets the clamp mask), g_next the gradient of next_s, g the gradient of s
- * (overwritten).  Body-pose gradients are added to bgrad / next_bgrad. */
-int dexmpm_substep_grad(const DexBatch *b, int epoch, const float *s, const float *next_s, const float *g_next,
+/* Adjoint of the substep whose forward (p2g + grid_op) filled grid slot
+ * `slot` from state s.  next_s is the state after the substep (its v sets the
+ * clamp mask), g_next the gradient of next_s, g the gradient of s
+ * (overwritten).  Body-pose gradients are added to bgrad / next_bgrad.  The
+ * slot is cleared for reuse. */
+int dexmpm_substep_grad(const DexBatch *b, int slot, const float *s, const float *next_s, const float *g_next,
                         float *g, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
                         dexmpm_stream_t stream);
 
-/* The three kernels of dexmpm_substep_grad, callable one by one (same
- * arguments): G2P adjoint (writes the x gradient of s and scatters
- * dL/dv_out), grid-update adjoint (dL/d(mv), dL/dm and body-pose gradients),
- * P2G + SVD adjoint (completes the gradient of s). */
-int dexmpm_g2p_grad(const DexBatch *b, int epoch, const float *s, const float *next_s, const float *g_next,
+/* The three kernels of dexmpm_substep_grad, callable one by one: G2P adjoint
+ * (writes the x gradient of s, scatters dL/dv_out), grid-update adjoint
+ * (dL/d(mv), dL/dm, body-pose gradients; clears the slot), P2G + SVD adjoint
+ * (completes the gradient of s). */
+int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *s, const float *next_s, const float *g_next,
                     float *g, dexmpm_stream_t stream);
-int dexmpm_grid_op_grad(const DexBatch *b, int epoch, const float *pose, const float *next_pose, float *bgrad,
+int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const float *next_pose, float *bgrad,
                         float *next_bgrad, dexmpm_stream_t stream);
-int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *s, const float *g_next, float *g,
+int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *s, const float *g_next, float *g,
                     dexmpm_stream_t stream);
 
 /* One forward substep (P2G, grid update, G2P) of ONE environment that
@@ -224,7 +231,7 @@ int dexmpm_p2g_grad(const DexBatch *b, int epoch, const float *s, const float *g
  *   error:  nullable device int32; DEXMPM_ERR_OUT_OF_GRID is OR-ed in when a
  *           particle stencil leaves the grid (that particle is skipped).
  * Grids, active-block lists and counters live in one fixed device array of
- * this library (12.7 MB, held by every GPU that loads it until exit), shared
+ * this library (8.5 MB, held by every GPU that loads it until exit), shared
  * by all calls: each call clears what must start at zero, and calls that
  * overlap on the GPU race on it.  The first call on a device looks up the
  * array's device address; make that first call before any stream capture.

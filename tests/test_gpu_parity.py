@@ -271,7 +271,7 @@ def test_graph_replay_equals_eager(cuda):
 
 def test_full_batch_properties(cuda):
     """64 envs x 50 substeps: finite, in bounds, no device error, and the
-    grid mass of every epoch equals the particle mass."""
+    grid mass of every substep equals the particle mass."""
     from dexdeform_gb300 import workloads as W
     from dexdeform_gb300.engine import BatchEngine, EnvSpec
     envs = W.batch_envs(0, n_envs=64, steps=50)
@@ -282,8 +282,8 @@ def test_full_batch_properties(cuda):
     nxt = E.new_slots(1)[0]
     total_mass = float(sum(e.mass.astype(np.float64).sum() for e in envs))
     for t in range(50):
-        E.substep(s, nxt, poses[t], poses[t + 1])
-        gm = float(E.grid[(E.epoch - 1) & 1][:, 3].double().sum())
+        slot = E.substep(s, nxt, poses[t], poses[t + 1])
+        gm = E.grid_mass(slot)
         assert abs(gm - total_mass) < 1e-4 * total_mass
         s, nxt = nxt, s
     assert E.error_word() == 0
