@@ -20,6 +20,7 @@
 // SVD and stress use the cancellation-free forms of mpm_math.cuh.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <climits>
 
 #include "mpm_math.cuh"
@@ -43,12 +44,21 @@ using namespace dexmpm;
 #ifndef DEX_NODE_UNROLL
 #define DEX_NODE_UNROLL 1
 #endif
+// Scatter reduction: 1 = transposed through shared memory, 0 = segmented
+// shuffles; warps with more than DEX_DIRECT_SEGS segments use plain atomics.
+#ifndef DEX_SCATTER
+#define DEX_SCATTER 1
+#endif
+#ifndef DEX_DIRECT_SEGS
+#define DEX_DIRECT_SEGS 8
+#endif
 constexpr int kNodeUnroll = DEX_NODE_UNROLL;
 
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int PX = 0, PV = 3, PF = 6, PC = 15;  // state plane offsets
+constexpr float kBlockReach = 2.6f;  // >= 1.5 sqrt(3): block centre to its farthest cell, in cells
 
 __device__ __forceinline__ f3 ldf3(const float *__restrict__ S, int N, int plane, int p) {
   return mk3(__ldg(S + (size_t)plane * N + p), __ldg(S + (size_t)(plane + 1) * N + p),
@@ -113,6 +123,7 @@ __device__ __forceinline__ void warp_sort(int &key, int &idx, int lane) {
   }
 }
 
+#if !DEX_SCATTER
 // Suffix sum within contiguous segments; the segment head ends with the total.
 __device__ __forceinline__ float seg_sum(float v, int lane, int seg_end) {
 #pragma unroll
@@ -122,6 +133,7 @@ __device__ __forceinline__ float seg_sum(float v, int lane, int seg_end) {
   }
   return v;
 }
+#endif
 
 __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, float d) {
   atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
@@ -131,6 +143,60 @@ __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
   return v;
+}
+
+// ------------------------------------------------ transposed warp scatter
+// The scatter kernels add 27 node contributions per particle to the grid.
+// Lanes are sorted by stencil base, so equal bases (same 27 target cells) are
+// contiguous segments.  Per group of up to 16 nodes every lane stores its
+// float4 per node in a per-warp shared buffer; then lane l owns component pair
+// (l & 1) of node (l >> 1), sums it over each segment with plain loads, and
+// the segment's total goes to the grid in one 8-byte vector atomic.  Rows are
+// padded to 132 floats so that both the stores (16 B per lane) and the loads
+// (8 B per lane, one row per lane pair) are free of bank conflicts.
+constexpr int kRedRow = 132;                 // floats per node row (32 lanes x 4 + 4 pad)
+constexpr int kRedWarpFloats = 16 * kRedRow;  // 16 node rows per warp
+constexpr int kDirectSegs = DEX_DIRECT_SEGS;  // more segments than this: per-lane atomics instead
+constexpr size_t kScatterSmemPerWarp = sizeof(float) * kRedWarpFloats;
+
+__device__ __forceinline__ float *warp_red_buffer() {
+  extern __shared__ float4 s_dyn[];
+  return reinterpret_cast<float *>(s_dyn) + (threadIdx.x >> 5) * kRedWarpFloats;
+}
+
+__device__ __forceinline__ void red_put(float *red, int c, int lane, float a, float b, float d, float e) {
+  *reinterpret_cast<float4 *>(red + c * kRedRow + 4 * lane) = make_float4(a, b, d, e);
+}
+
+// Sum the stored rows of nodes node0 .. node0 + n_nodes - 1 over every segment
+// (heads: lanes starting a segment; n_live: live lanes, which come first) and
+// add them at the segment's stencil base + node offset.  Warp-uniform.
+__device__ __forceinline__ void red_walk(const float *red, unsigned heads, int n_live, int node0, int n_nodes,
+                                         const int base[3], const DexEnv &E, float *grid, int lane) {
+  const int c = lane >> 1, h = lane & 1;
+  const int n = node0 + c;
+  const bool act = c < n_nodes;
+  const int ni = n / 9, nj = (n / 3) % 3, nk = n % 3;
+  const float *col = red + c * kRedRow + 2 * h;
+  unsigned rest = heads;
+  while (rest) {
+    const int start = __ffs(rest) - 1;
+    rest &= rest - 1u;
+    const int end = rest ? __ffs(rest) - 1 : n_live;
+    const int bx = __shfl_sync(kFull, base[0], start);
+    const int by = __shfl_sync(kFull, base[1], start);
+    const int bz = __shfl_sync(kFull, base[2], start);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int q = start; q < end; ++q) {
+      const float2 t = *reinterpret_cast<const float2 *>(col + 4 * q);
+      acc.x += t.x;
+      acc.y += t.y;
+    }
+    if (act) {
+      const int ci = cell_index(E, bx + ni, by + nj, bz + nk);
+      atomicAdd(reinterpret_cast<float2 *>(grid + 4 * (size_t)ci + 2 * h), acc);
+    }
+  }
 }
 
 __device__ __forceinline__ void mark_block(const DexBatch &B, int X, int blk) {
@@ -154,6 +220,25 @@ __device__ __forceinline__ void load_shape(const float *__restrict__ S, int b, B
   float4 q = __ldg(reinterpret_cast<const float4 *>(S) + 2 * b + 1);
   o.tfsr = mkq(a.x, a.y, a.z, a.w);
   o.args = mkq(q.x, q.y, q.z, q.w);
+}
+
+// Bodies of env E that can touch some cell of the 4^3 block (bx, by, bz)
+// (body_may_touch with the block centre and its half-diagonal 1.5 sqrt(3) dx):
+// bit b for body b, the same in every lane of the warp (one lane per body).
+// Skipping the other bodies leaves every node of the block as it was.
+__device__ __forceinline__ uint32_t bodies_near_block(const DexBatch &B, const DexEnv &E, const float *__restrict__ pose,
+                                                      int bx, int by, int bz, int nbod) {
+  const int lane = threadIdx.x & 31;
+  bool near = false;
+  if (lane < nbod) {
+    BodyPose cur;
+    BodyShape sh;
+    load_pose(pose, E.body_off + lane, cur);
+    load_shape(B.body_shape, E.body_off + lane, sh);
+    const f3 c = mk3((4 * bx + 1.5f) * E.dx, (4 * by + 1.5f) * E.dx, (4 * bz + 1.5f) * E.dx);
+    near = body_may_touch(c, kBlockReach * E.dx, cur, sh);
+  }
+  return __ballot_sync(kFull, near);
 }
 
 // Per-lane particle selection shared by the scatter kernels: lanes are sorted
@@ -229,6 +314,48 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
   make_stencil(x, E.inv_dx, st);
   float *grid = slot_grid(B, X);
 
+#if DEX_SCATTER
+  const unsigned heads = __ballot_sync(kFull, L.head);
+  const int n_live = __popc(__ballot_sync(kFull, L.live));
+  if (__popc(heads) > kDirectSegs) {
+    // nearly one particle per cell: per-lane vector atomics
+#pragma unroll kNodeUnroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+          const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
+                              ((float)k - st.fx[2]) * E.dx);
+          const f3 c = (mom + mv(A, dpos)) * w;
+          if (L.live) {
+            const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+            red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, m * w);
+          }
+        }
+  } else {
+    float *red = warp_red_buffer();
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int n = 16 * g + c;
+        if (n < 27) {
+          const int i = n / 9, j = (n / 3) % 3, k = n % 3;
+          const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+          const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
+                              ((float)k - st.fx[2]) * E.dx);
+          const f3 cv = (mom + mv(A, dpos)) * w;
+          red_put(red, c, lane, cv.x, cv.y, cv.z, m * w);
+        }
+      }
+      __syncwarp();
+      red_walk(red, heads, n_live, 16 * g, g == 0 ? 16 : 11, st.base, E, grid, lane);
+      __syncwarp();
+    }
+  }
+#else
 #pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -251,6 +378,7 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
           red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, cm);
         }
       }
+#endif
 
   if (L.head) {
     const int nby = E.gy >> 2, nbz = E.gz >> 2;
@@ -284,12 +412,14 @@ __global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, int Y, const
     const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
     const int ci = (blk << 6) + cell;
     const float4 g = grid[ci];
+    const uint32_t near = bodies_near_block(B, E, pose, bx, by, bz, E.n_bodies);
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
     if (g.w > kMassEps) {
       const float inv_m = 1.f / g.w;
       f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
       const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
-      for (int b = 0; b < E.n_bodies; ++b) {
+      for (uint32_t rest = near; rest; rest &= rest - 1u) {
+        const int b = __ffs(rest) - 1;
         BodyPose cur, nxt;
         BodyShape sh;
         load_pose(pose, E.body_off + b, cur);
@@ -398,31 +528,71 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   float *vg = B.vout_grad;
   const float c4 = 4.f * E.inv_dx;
+  // one stencil node: gather-side gradient terms into gx; returns the node's
+  // dL/dv_out contribution
+  auto node = [&](int i, int j, int k, int ci) -> f3 {
+    const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+    const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
+    const float4 g4 = L.live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const f3 gv = mk3(g4.x, g4.y, g4.z);
+    const float xx = w * c4;
+    gx += mtv(gC, gv) * (-E.inv_dx * xx);
+    const float gw = dot(gnv, gv) + c4 * dot(gv, mv(gC, dpos));
+    const f3 dw = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
+                      st.w[0][i] * st.w[1][j] * w1[2][k]);
+    gx += dw * gw;
+    return gnv * w + mv(gC, dpos) * xx;
+  };
+#if DEX_SCATTER
+  const unsigned heads = __ballot_sync(kFull, L.head);
+  const int n_live = __popc(__ballot_sync(kFull, L.live));
+  if (__popc(heads) > kDirectSegs) {
+#pragma unroll kNodeUnroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+          const f3 ggv = node(i, j, k, ci);
+          if (L.live) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
+        }
+  } else {
+    float *red = warp_red_buffer();
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int n = 16 * g + c;
+        if (n < 27) {
+          const int i = n / 9, j = (n / 3) % 3, k = n % 3;
+          const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+          const f3 ggv = node(i, j, k, ci);
+          red_put(red, c, lane, ggv.x, ggv.y, ggv.z, 0.f);
+        }
+      }
+      __syncwarp();
+      red_walk(red, heads, n_live, 16 * g, g == 0 ? 16 : 11, st.base, E, vg, lane);
+      __syncwarp();
+    }
+  }
+#else
 #pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
         const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
-        const float4 g4 = L.live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const f3 gv = mk3(g4.x, g4.y, g4.z);
-        const float xx = w * c4;
-        f3 ggv = gnv * w + mv(gC, dpos) * xx;
+        f3 ggv = node(i, j, k, ci);
         if (!L.lone) {
           ggv.x = seg_sum(ggv.x, lane, L.seg_end);
           ggv.y = seg_sum(ggv.y, lane, L.seg_end);
           ggv.z = seg_sum(ggv.z, lane, L.seg_end);
         }
         if (L.head) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
-        gx += mtv(gC, gv) * (-E.inv_dx * xx);
-        const float gw = dot(gnv, gv) + c4 * dot(gv, mv(gC, dpos));
-        const f3 dw = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
-                          st.w[0][i] * st.w[1][j] * w1[2][k]);
-        gx += dw * gw;
       }
+#endif
   if (L.live) stf3(G, N, PX, p, gx);
 }
 
@@ -470,8 +640,10 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
     uint32_t touched = 0u;
     f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
     const int nbod = in_list ? E.n_bodies : 0;
+    const uint32_t near = bodies_near_block(B, E, pose, bx, by, bz, nbod);
     if (active) {
-      for (int b = 0; b < nbod; ++b) {
+      for (uint32_t rest = near; rest; rest &= rest - 1u) {
+        const int b = __ffs(rest) - 1;
         BodyPose cur, nxt;
         BodyShape sh;
         load_pose(pose, E.body_off + b, cur);
@@ -487,7 +659,8 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
     const float4 gv4 = active ? vgrad[ci] : z4;
     f3 gv = boundary_backward(mk3(gv4.x, gv4.y, gv4.z), v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
     // the warp's lanes share one block, hence one env and one body count
-    for (int b = nbod - 1; b >= 0; --b) {
+    for (uint32_t rest = near; rest; rest &= ~(1u << (31 - __clz(rest)))) {
+      const int b = 31 - __clz(rest);
       const bool hit = (touched >> b) & 1u;
       if (!__any_sync(kFull, hit)) continue;
       float gc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -650,6 +823,24 @@ bool valid(const DexBatch *b) {
          b->grid_ctas > 0;
 }
 bool slot_ok(const DexBatch *b, int k) { return k >= 0 && k < b->n_slots; }
+
+// Dynamic shared memory of the scatter kernels for CTAs of `threads`.
+size_t scatter_smem(int threads) { return DEX_SCATTER ? (size_t)(threads / 32) * kScatterSmemPerWarp : 0; }
+
+// Opt the scatter kernels in to the dynamic shared memory of 256-thread CTAs
+// (above the 48 KB default), once per device.
+int scatter_attr_ready() {
+  static std::atomic<int> ready[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEXMPM_ERR_LAUNCH;
+  if (ready[dev].load(std::memory_order_acquire)) return DEXMPM_OK;
+  const int bytes = (int)scatter_smem(256);
+  if (cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k_g2p_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+    return DEXMPM_ERR_LAUNCH;
+  ready[dev].store(1, std::memory_order_release);
+  return DEXMPM_OK;
+}
 bool grad_ok(const DexBatch *b) { return valid(b) && b->vout_grad && b->in_grad; }
 
 }  // namespace
@@ -669,13 +860,15 @@ int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream) {
   if (cudaMemsetAsync(b->block_flag, 0, (size_t)b->n_blocks * b->n_slots * sizeof(uint32_t), s) != cudaSuccess)
     return DEXMPM_ERR_LAUNCH;
   k_reset_counts<<<1, 256, 0, s>>>(*b);
-  return check_launch();
+  if (int rc = check_launch()) return rc;
+  return scatter_attr_ready();
 }
 
 int dexmpm_p2g(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm_stream_t stream) {
   if (!valid(b) || !S || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_p2g<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext);
+  if (int rc = scatter_attr_ready()) return rc;
+  k_p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext);
   return check_launch();
 }
 
@@ -709,7 +902,9 @@ int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *S, const float *Sn
                     dexmpm_stream_t stream) {
   if (!grad_ok(b) || !S || !Snext || !Gnext || !G || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_g2p_grad<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext, Gnext, G);
+  if (int rc = scatter_attr_ready()) return rc;
+  k_g2p_grad<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext, Gnext,
+                                                                                           G);
   return check_launch();
 }
 

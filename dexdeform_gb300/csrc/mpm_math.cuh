@@ -503,6 +503,23 @@ DX_HD bool contact_forward(f3 gx, f3 &v, const BodyPose &cur, const BodyPose &nx
   return true;
 }
 
+// Whether a body can touch any grid node within distance `reach` of `centre`.
+// A contact changes a node's velocity only where its signed distance d
+// satisfies d <= 0 or exp(-softness d) > 0.1, i.e. d < ln(10) / softness
+// (integrator.cu:700-712).  The body-frame map x -> q^-1 (x - p) has operator
+// norm at most |1 - |q|^2| + |q|^2 (1 for a unit quaternion) and the box and
+// capsule distances are 1-Lipschitz, so a node whose distance exceeds the
+// cutoff at the centre by more than norm x reach is untouched.  A margin of
+// 0.1% + 1e-5 covers FP32 rounding; a NaN distance keeps the body.
+DX_HD bool body_may_touch(f3 centre, float reach, const BodyPose &cur, const BodyShape &sh) {
+  const float d = shape_sdf(sh.tfsr, sh.args, xform_inv(cur.p, cur.q, centre));
+  const float qn = cur.q.w * cur.q.w + cur.q.x * cur.q.x + cur.q.y * cur.q.y + cur.q.z * cur.q.z;
+  const float lip = fabsf(1.f - qn) + qn;
+  const float soft = sh.tfsr.y;
+  const float cutoff = soft > 0.f ? 2.30258509f / soft : 0.f;
+  return !(d - lip * reach > cutoff * 1.001f + 1e-5f);
+}
+
 // Walls and ground after the contacts (integrator.cu:734-774).
 DX_HD f3 boundary_forward(f3 v, int gx, int gy, int gz, int Gx, int Gy, int Gz, float ground_friction) {
   if (gx < kBound && v.x < 0.f) v.x = 0.f;

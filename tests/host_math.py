@@ -68,3 +68,15 @@ def substep(env, st, t):
                    _p(f32(env.gravity)), ctypes.c_float(env.ground_friction), ctypes.c_int(env.nb), _p(pose),
                    _p(npose), _p(shapes), _p(out["x"]), _p(out["v"]), _p(out["F"]), _p(out["C"]))
     return out
+
+
+def block_cull(pose, shapes, blk, dx):
+    """(may, touched) per case of the block culling test (see math_host.cpp)."""
+    L = load()
+    pose, shapes = f32(pose), f32(shapes)
+    blk = np.ascontiguousarray(blk, np.int32)
+    n = pose.shape[0]
+    may, touched = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    L.host_block_cull(ctypes.c_int(n), _p(pose), _p(shapes), blk.ctypes.data_as(ctypes.c_void_p), ctypes.c_float(dx),
+                      may.ctypes.data_as(ctypes.c_void_p), touched.ctypes.data_as(ctypes.c_void_p))
+    return may.astype(bool), touched.astype(bool)

@@ -104,3 +104,31 @@ extern "C" void host_substep(int n, const float *x, const float *v, const float 
     store9(oC + 9 * p, nC);
   }
 }
+
+// Block culling check: for case c, a body (pose [8], shape [8]) and a 4^3
+// block with origin cell blk[3c..3c+2].  may[c] = the block test's answer;
+// touched[c] = 1 if contact_forward's activation holds at any of the 64 cells.
+extern "C" void host_block_cull(int n, const float *pose, const float *shapes, const int *blk, float dx, int *may,
+                                int *touched) {
+  for (int c = 0; c < n; ++c) {
+    BodyPose cur;
+    cur.p = mk3(pose[8 * c], pose[8 * c + 1], pose[8 * c + 2]);
+    cur.q = mkq(pose[8 * c + 4], pose[8 * c + 5], pose[8 * c + 6], pose[8 * c + 7]);
+    BodyShape sh;
+    sh.tfsr = mkq(shapes[8 * c], shapes[8 * c + 1], shapes[8 * c + 2], shapes[8 * c + 3]);
+    sh.args = mkq(shapes[8 * c + 4], shapes[8 * c + 5], shapes[8 * c + 6], shapes[8 * c + 7]);
+    const int bx = blk[3 * c], by = blk[3 * c + 1], bz = blk[3 * c + 2];
+    f3 centre = mk3((bx + 1.5f) * dx, (by + 1.5f) * dx, (bz + 1.5f) * dx);
+    may[c] = body_may_touch(centre, 2.6f * dx, cur, sh) ? 1 : 0;
+    int t = 0;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 4; ++k) {
+          f3 g = mk3((bx + i) * dx, (by + j) * dx, (bz + k) * dx);
+          float dist = shape_sdf(sh.tfsr, sh.args, xform_inv(cur.p, cur.q, g));
+          float infl = fminf(expf(-dist * sh.tfsr.y), 1.f);
+          if ((sh.tfsr.y > 0.f && infl > 0.1f) || dist <= 0.f) t = 1;
+        }
+    touched[c] = t;
+  }
+}

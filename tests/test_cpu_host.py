@@ -138,3 +138,33 @@ def test_workloads_are_seeded_and_in_range():
         assert v.max() <= 0.5 + 1e-3
         q = np.linalg.norm(e.poses[:, :, 3:], axis=-1)
         assert np.abs(q - 1).max() < 1e-5
+
+
+def test_block_culling_never_skips_a_touching_body():
+    """The grid kernels skip a body for a whole 4^3 block when a distance
+    bound at the block centre proves no cell of the block is in contact.
+    Check the bound against the contact activation at all 64 cells, for
+    capsules and boxes, unit and non-unit quaternions, several softness
+    values and rounding radii."""
+    rng = np.random.default_rng(7)
+    n, dx = 60000, 1.0 / 64
+    pose = np.zeros((n, 8), np.float32)
+    pose[:, :3] = rng.uniform(0.3, 0.7, (n, 3))
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q *= rng.choice([1.0, 1.0, 1.0, 0.9, 1.15], size=(n, 1))
+    pose[:, 4:] = q
+    shapes = np.zeros((n, 8), np.float32)
+    shapes[:, 0] = rng.integers(0, 2, n)
+    shapes[:, 1] = 0.9
+    shapes[:, 2] = rng.choice([666.0, 50.0, 5000.0, 0.0], n)
+    shapes[:, 3] = rng.choice([0.0, 0.005], n)
+    cap = shapes[:, 0] == 1
+    shapes[cap, 4] = rng.uniform(0.008, 0.02, cap.sum())
+    shapes[cap, 5] = rng.uniform(0.02, 0.05, cap.sum())
+    shapes[~cap, 4:7] = rng.uniform(0.01, 0.05, ((~cap).sum(), 3))
+    blk = (np.floor(pose[:, :3] / dx / 4) * 4 + 4 * rng.integers(-3, 3, (n, 3))).astype(np.int32)
+    import host_math as H
+    may, touched = H.block_cull(pose, shapes, blk, dx)
+    assert not np.any(touched & ~may)
+    assert touched.sum() > 1000 and (~may).sum() > 0.3 * n
