@@ -331,7 +331,8 @@ def kernel_times(E, R, s0, g_final):
     src = ck[0]
     for s in range(T):
         slot, dst = 2 + s, ring[s + 1]
-        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "p2g"))
+        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), N.ptr(R._tape(s)), sp),
+                                     "p2g"))
         timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, -1, N.ptr(R.poses[s]), N.ptr(R.poses[s + 1]),
                                                           sp), "grid_op"))
         timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
@@ -350,8 +351,8 @@ def kernel_times(E, R, s0, g_final):
         timed("grid_op_grad", lambda: N.check(L.dexmpm_grid_op_grad(E._bp, slot, N.ptr(pz), N.ptr(pn),
                                                                     N.ptr(R.bgrad[s]), N.ptr(R.bgrad[s + 1]), sp),
                                               "grid_op_grad"))
-        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, slot, N.ptr(cur), N.ptr(gn), N.ptr(g), sp),
-                                          "p2g_grad"))
+        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, slot, N.ptr(cur), N.ptr(gn), N.ptr(g),
+                                                            N.ptr(R._tape(s)), sp), "p2g_grad"))
         gn, g = g, gn
     torch.cuda.synchronize()
     return {k: 1e3 * sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in acc.items()}, cells

@@ -58,14 +58,14 @@ _REF_SIGS = {
 }
 _BATCH_SIGS = {
     "dexmpm_reset": [POINTER(DexBatch), P],
-    "dexmpm_p2g": [POINTER(DexBatch), c_int, P, P, P],
+    "dexmpm_p2g": [POINTER(DexBatch), c_int, P, P, P, P],
     "dexmpm_grid_op": [POINTER(DexBatch), c_int, c_int, P, P, P],
     "dexmpm_g2p": [POINTER(DexBatch), c_int, P, P, P],
-    "dexmpm_substep": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P],
-    "dexmpm_substep_grad": [POINTER(DexBatch), c_int, P, P, P, P, P, P, P, P, P],
+    "dexmpm_substep": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P, P],
+    "dexmpm_substep_grad": [POINTER(DexBatch), c_int, P, P, P, P, P, P, P, P, P, P],
     "dexmpm_g2p_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
     "dexmpm_grid_op_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
-    "dexmpm_p2g_grad": [POINTER(DexBatch), c_int, P, P, P, P],
+    "dexmpm_p2g_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
     "dexmpm_get_error": [POINTER(DexBatch), POINTER(c_int32), P],
     "dexmpm_substep_noalloc": [POINTER(DexEnv), P, P, P, P, P, P, P, P, P, P],
     "dexmpm_abi_get_error": [POINTER(c_int32)],

@@ -80,6 +80,30 @@ __device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m
   for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
 }
 
+// SVD tape: the recomputed forward P2G stores each particle's SVD of F_tmp in
+// 24 planes (U 0-8, V 9-17, sigma 18-20, sigma - 1 21-23) so that the P2G
+// adjoint reads it instead of repeating the SVD.
+__device__ __forceinline__ void store_svd(float *T, int N, int p, const SVD3 &sv) {
+  stm33(T, N, 0, p, sv.U);
+  stm33(T, N, 9, p, sv.V);
+  stf3(T, N, 18, p, sv.s);
+  stf3(T, N, 21, p, sv.d);
+}
+__device__ __forceinline__ SVD3 load_svd(const float *__restrict__ T, int N, int p) {
+  SVD3 sv;
+  sv.U = ldm33(T, N, 0, p);
+  sv.V = ldm33(T, N, 9, p);
+  sv.s = ldf3(T, N, 18, p);
+  sv.d = ldf3(T, N, 21, p);
+  return sv;
+}
+
+// Stencil-node arithmetic: affine terms M dpos are built from M's columns,
+// M ((i, j, k) - fx) h = m0 + i h M0 + j h M1 + k h M2 with m0 = -h M fx, one
+// step per axis (folded to nothing / an add when the offset is a constant).
+__device__ __forceinline__ f3 step3(f3 a, f3 c, int i) { return i == 0 ? a : (i == 1 ? a + c : a + c * 2.f); }
+__device__ __forceinline__ f3 mcol(const m33 &M, int c) { return mk3(M.a[0][c], M.a[1][c], M.a[2][c]); }
+
 __device__ __forceinline__ float *slot_grid(const DexBatch &B, int k) {
   return B.grid + (size_t)k * B.n_blocks * 256;  // 64 cells x float4 per block
 }
@@ -281,7 +305,7 @@ __device__ __forceinline__ Lane sorted_lane(const DexBatch &B, const DexEnv &E, 
 // =================================================================== P2G
 // integrator.cu:84-100 (compute_svd) fused with :312-394 (p2g).
 __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, const float *__restrict__ S,
-                                             float *__restrict__ Snext) {
+                                             float *__restrict__ Snext, float *__restrict__ tape) {
   const int tile = blockIdx.x;
   const DexEnv E = B.envs[B.tiles[2 * tile]];
   const int first = B.tiles[2 * tile + 1];
@@ -305,6 +329,7 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
   Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
   const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
   if (Snext != nullptr && L.live) stm33(Snext, N, PF, p, pl.newF);
+  if (tape != nullptr && L.live) store_svd(tape, N, p, sv);
 
   const float scale = L.live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
   const m33 A = pl.P * scale + C * m;
@@ -528,20 +553,23 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   float *vg = B.vout_grad;
   const float c4 = 4.f * E.inv_dx;
+  // gC dpos (dpos in cells) = q0 + i gC0 + j gC1 + k gC2
+  const f3 g0c = mcol(gC, 0), g1c = mcol(gC, 1), g2c = mcol(gC, 2);
+  const f3 q0 = -(g0c * st.fx[0] + g1c * st.fx[1] + g2c * st.fx[2]);
+  f3 wgv = mk3(0.f, 0.f, 0.f);  // sum of w v_out over the nodes
   // one stencil node: gather-side gradient terms into gx; returns the node's
   // dL/dv_out contribution
   auto node = [&](int i, int j, int k, int ci) -> f3 {
     const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-    const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
+    const f3 gCd = step3(step3(step3(q0, g0c, i), g1c, j), g2c, k);
     const float4 g4 = L.live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
     const f3 gv = mk3(g4.x, g4.y, g4.z);
-    const float xx = w * c4;
-    gx += mtv(gC, gv) * (-E.inv_dx * xx);
-    const float gw = dot(gnv, gv) + c4 * dot(gv, mv(gC, dpos));
+    wgv += gv * w;
+    const float gw = dot(gnv, gv) + c4 * dot(gv, gCd);
     const f3 dw = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
                       st.w[0][i] * st.w[1][j] * w1[2][k]);
     gx += dw * gw;
-    return gnv * w + mv(gC, dpos) * xx;
+    return gnv * w + gCd * (w * c4);
   };
 #if DEX_SCATTER
   const unsigned heads = __ballot_sync(kFull, L.head);
@@ -593,6 +621,8 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
         if (L.head) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
       }
 #endif
+  // the C-gradient term of every node: sum_n gC^T v_n (-inv_dx c4 w_n)
+  gx += mtv(gC, wgv) * (-E.inv_dx * c4);
   if (L.live) stf3(G, N, PX, p, gx);
 }
 
@@ -707,9 +737,12 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
 // ============================================================ P2G adjoint
 // integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad).
 // Adds to the x gradient written by k_g2p_grad and writes v, F, C gradients.
+// With kTape the SVD of F_tmp comes from the tape the recomputed forward
+// wrote (same values, without the SVD's registers and arithmetic).
+template <bool kTape>
 __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
                                                   const float *__restrict__ Gnext, float *__restrict__ G,
-                                                  int split) {
+                                                  int split, const float *__restrict__ tape) {
   const int tile = blockIdx.x / split, part = blockIdx.x % split;
   const DexEnv E = B.envs[B.tiles[2 * tile]];
   const int first = B.tiles[2 * tile + 1];
@@ -728,7 +761,7 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
               ys = __ldg(B.mu_lam_yield + 2 * N + p);
   const m33 Et = deviation_tmp(F, C, E.dt);
-  const SVD3 sv = svd3_from_deviation(Et);
+  const SVD3 sv = kTape ? load_svd(tape, N, p) : svd3_from_deviation(Et);
   m33 Ft = Et;
   Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
   const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
@@ -738,8 +771,20 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
   const float4 *__restrict__ ig = reinterpret_cast<const float4 *>(B.in_grad);
-  m33 g_stress = mzero(), g_C = mzero();
-  f3 g_x = mk3(0.f, 0.f, 0.f), g_v = mk3(0.f, 0.f, 0.f);
+  // per node n with weight N_n, offset dpos_n and incoming dL/d(mv), dL/dm
+  // (gov_n, gm_n):  dL/dstress = gss Gs, dL/dC = m Gs with Gs = sum N gov dpos^T;
+  // dL/dv = m sum N gov; dL/dx = sum dN (m gm + m v.gov + gov.(A dpos)) - A^T sum N gov.
+  // A dpos = a0 + i A0 dx + j A1 dx + k A2 dx.
+  const f3 a0c = mcol(A, 0) * E.dx, a1c = mcol(A, 1) * E.dx, a2c = mcol(A, 2) * E.dx;
+  const f3 a0 = -(a0c * st.fx[0] + a1c * st.fx[1] + a2c * st.fx[2]);
+  float dp[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dp[d][i] = ((float)i - st.fx[d]) * E.dx;
+  const f3 u = v * m;
+  m33 Gs = mzero();
+  f3 g_x = mk3(0.f, 0.f, 0.f), gw = mk3(0.f, 0.f, 0.f);
 #pragma unroll kNodeUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -747,18 +792,19 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const float Nw = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx, ((float)k - st.fx[2]) * E.dx);
         const float4 g4 = __ldg(ig + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k));
         const f3 gov = mk3(g4.x, g4.y, g4.z);
         const f3 gN = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
                           st.w[0][i] * st.w[1][j] * w1[2][k]);
-        const m33 tmp = outer(gov, dpos);
-        g_stress += tmp * (Nw * gss);
-        g_C += tmp * (Nw * m);
-        g_v += gov * (Nw * m);
-        g_x += gN * (g4.w * m + dot(v, gov) * m + dot(mv(A, dpos), gov));
-        g_x -= mtv(A, gov) * Nw;
+        const f3 Ad = step3(step3(step3(a0, a0c, i), a1c, j), a2c, k);
+        const f3 a = gov * Nw;
+        Gs += outer(a, mk3(dp[0][i], dp[1][j], dp[2][k]));
+        gw += a;
+        g_x += gN * (g4.w * m + dot(u, gov) + dot(Ad, gov));
       }
+  g_x -= mtv(A, gw);
+  const m33 g_stress = Gs * gss, g_C = Gs * m;
+  const f3 g_v = gw * m;
 
   // stress -> (U, V, sigma, F_tmp) gradients (integrator.cu:541-625)
   const m33 &nF = pl.newF;
@@ -864,11 +910,11 @@ int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream) {
   return scatter_attr_ready();
 }
 
-int dexmpm_p2g(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm_stream_t stream) {
+int dexmpm_p2g(const DexBatch *b, int slot, const float *S, float *Snext, float *tape, dexmpm_stream_t stream) {
   if (!valid(b) || !S || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   if (int rc = scatter_attr_ready()) return rc;
-  k_p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext);
+  k_p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext, tape);
   return check_launch();
 }
 
@@ -890,8 +936,8 @@ int dexmpm_g2p(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm
 }
 
 int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *S, float *Snext, const float *pose,
-                   const float *next_pose, dexmpm_stream_t stream) {
-  int rc = dexmpm_p2g(b, slot, S, Snext, stream);
+                   const float *next_pose, float *tape, dexmpm_stream_t stream) {
+  int rc = dexmpm_p2g(b, slot, S, Snext, tape, stream);
   if (rc) return rc;
   rc = dexmpm_grid_op(b, slot, clear_slot, pose, next_pose, stream);
   if (rc) return rc;
@@ -916,25 +962,28 @@ int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const fl
   return check_launch();
 }
 
-int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gnext, float *G,
+int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gnext, float *G, const float *tape,
                     dexmpm_stream_t stream) {
   if (!grad_ok(b) || !S || !Gnext || !G || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   // the adjoint is register-heavy: 128-thread CTAs, tile_size/128 of them per tile
   const int cta = b->tile_size < 128 ? b->tile_size : 128;
   const int split = b->tile_size / cta;
-  k_p2g_grad<<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split);
+  if (tape)
+    k_p2g_grad<true><<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split, tape);
+  else
+    k_p2g_grad<false><<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split, nullptr);
   return check_launch();
 }
 
 int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float *Snext, const float *Gnext,
                         float *G, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
-                        dexmpm_stream_t stream) {
+                        const float *tape, dexmpm_stream_t stream) {
   int rc = dexmpm_g2p_grad(b, slot, S, Snext, Gnext, G, stream);
   if (rc) return rc;
   rc = dexmpm_grid_op_grad(b, slot, pose, next_pose, bgrad, next_bgrad, stream);
   if (rc) return rc;
-  return dexmpm_p2g_grad(b, slot, S, Gnext, G, stream);
+  return dexmpm_p2g_grad(b, slot, S, Gnext, G, tape, stream);
 }
 
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {

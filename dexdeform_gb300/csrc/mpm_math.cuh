@@ -289,13 +289,39 @@ struct SVD3 {
   f3 s, d;
 };
 
+// Reciprocal square root and division for rotation parameters, where a few
+// ulp of error only perturb an angle: the hardware approximations on the GPU
+// (callers keep the arguments finite and away from denormals), exact on the host.
+DX_HD float rot_rsqrt(float x) {
+#ifdef __CUDA_ARCH__
+  return rsqrtf(x);
+#else
+  return 1.f / sqrtf(x);
+#endif
+}
+DX_HD float rot_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// One Jacobi rotation zeroing S[p][q].  Skipped when the pivot is below FP32
+// resolution of the diagonal pair (a rotation could change the eigenvalues by
+// at most that, relative) or below 1e-30 in absolute terms.  The tangent is
+// t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)), theta = (S_qq - S_pp) / (2 S_pq),
+// with |theta| capped at 1e18 (t below 5e-19 is no rotation at FP32).
 DX_HD void jacobi_rotate(float S[3][3], m33 &V, int p, int q, int r) {
   float apq = S[p][q];
-  if (apq == 0.f) return;
-  float theta = (S[q][q] - S[p][p]) / (2.f * apq);
-  float t = 1.f / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+  const float app = S[p][p], aqq = S[q][q];
+  if (!(fabsf(apq) > fmaxf(5.9604645e-8f * fmaxf(fabsf(app), fabsf(aqq)), 1e-30f))) return;
+  float theta = rot_div(aqq - app, 2.f * apq);
+  const float at = fminf(fabsf(theta), 1e18f);
+  const float sq = at * at + 1.f;
+  float t = rot_div(1.f, at + sq * rot_rsqrt(sq));
   t = theta < 0.f ? -t : t;
-  float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+  float c = rot_rsqrt(t * t + 1.f), s = t * c;
   S[p][p] -= t * apq;
   S[q][q] += t * apq;
   S[p][q] = S[q][p] = 0.f;
@@ -322,9 +348,10 @@ DX_HD void swap_neg_cols(m33 &M, int i, int j) {
 // Givens rotation on rows (i, j) zeroing B[j][col]; U accumulates G^T.
 DX_HD void qr_rotate(m33 &B, m33 &U, int i, int j, int col) {
   float a = B.a[i][col], b = B.a[j][col];
-  float r = sqrtf(a * a + b * b);
-  if (!(r > 0.f)) return;
-  float c = a / r, s = b / r;
+  const float r2 = a * a + b * b;
+  if (!(r2 > 1e-36f)) return;
+  const float ir = rot_rsqrt(r2);
+  float c = a * ir, s = b * ir;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float bi = B.a[i][k], bj = B.a[j][k];
@@ -338,7 +365,7 @@ DX_HD void qr_rotate(m33 &B, m33 &U, int i, int j, int col) {
 
 DX_HD float sig_minus_one(float lam) {
   float l = fmaxf(lam, -1.f);
-  return l / (1.f + sqrtf(1.f + l));
+  return rot_div(l, 1.f + sqrtf(1.f + l));
 }
 
 DX_HD SVD3 svd3_from_deviation(const m33 &E) {

@@ -147,5 +147,5 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   b.body_shape = body_shape;
   b.error = error ? error : reinterpret_cast<int32_t *>(base + kCounts + 12);
   // one grid slot, nothing to clear afterwards (the next call re-zeroes it)
-  return dexmpm_substep(&b, 0, -1, s, next_s, pose, next_pose, stream);
+  return dexmpm_substep(&b, 0, -1, s, next_s, pose, next_pose, nullptr, stream);
 }

@@ -68,14 +68,14 @@ def footprint_bytes(specs: Sequence[EnvSpec], n_slots: int = 2, grad: bool = Fal
                     env_steps: int = 0) -> int:
     """Device bytes a batch needs (used by admission control): grid slots
     (2, plus one per substep of an env step with gradients), state slots,
-    checkpoints and poses."""
+    checkpoints, the SVD tape of one env step (gradients) and poses."""
     n = sum(s.n for s in specs)
     blocks = sum((s.grid_dim[0] // 4) * (s.grid_dim[1] // 4) * (s.grid_dim[2] // 4) for s in specs)
     nb = sum(s.nb for s in specs)
     grid_slots = 2 + (substeps if grad else 0)
     b = blocks * 64 * 32 * grid_slots + blocks * 8 * grid_slots + blocks * 4
     b += blocks * 64 * 32 if grad else 0
-    slots = n_slots + ((env_steps + 1) + (substeps + 1) + 2 if grad else 0)
+    slots = n_slots + ((env_steps + 1) + (substeps + 1) + 2 + substeps if grad else 0)
     b += slots * 24 * 4 * n + 5 * 4 * n
     b += (env_steps * substeps + 1) * nb * 32 * (2 if grad else 1)
     return int(b)
@@ -228,11 +228,12 @@ class BatchEngine:
 
     # ------------------------------------------------------------ kernels
     def substep(self, s: torch.Tensor, s_next: torch.Tensor, pose: torch.Tensor, next_pose: torch.Tensor,
-                slot: Optional[int] = None):
+                slot: Optional[int] = None, tape: Optional[torch.Tensor] = None):
         """One forward substep (P2G, grid update, G2P) of every env.  Without
         `slot` it uses the forward slot pair (alternating, each clearing the
         other); with `slot` (>= 2) it fills that grid slot and keeps it for the
-        adjoint of this substep."""
+        adjoint of this substep.  `tape` (a state-shaped slot) receives the
+        SVD of every particle for that adjoint."""
         if slot is None:
             slot, clear = self.fslot, self.fslot ^ 1
             self.fslot ^= 1
@@ -240,26 +241,30 @@ class BatchEngine:
             assert 2 <= slot < self.n_grid_slots
             clear = -1
         N.check(self.lib.dexmpm_substep(self._bp, slot, clear, N.ptr(s), N.ptr(s_next), N.ptr(pose),
-                                        N.ptr(next_pose), N.stream_ptr()), "dexmpm_substep")
+                                        N.ptr(next_pose), N.ptr(tape), N.stream_ptr()), "dexmpm_substep")
         self.launches += 3
         return slot
 
-    def substep_grad(self, s, s_next, g_next, g, pose, next_pose, bgrad, next_bgrad, slot: Optional[int] = None):
+    def substep_grad(self, s, s_next, g_next, g, pose, next_pose, bgrad, next_bgrad, slot: Optional[int] = None,
+                     tape: Optional[torch.Tensor] = None):
         """Adjoint of one substep: G2P, grid and P2G adjoints.  With `slot` the
         grid slot left by that substep's forward is used (and cleared);
-        without, P2G and the grid update are recomputed from s first.
+        without, P2G and the grid update are recomputed from s first.  With
+        `tape` (written by that forward) the SVD is read, not recomputed.
         g (gradient of s) is overwritten."""
         assert self.grad, "engine built without gradient buffers"
         sp = N.stream_ptr()
         if slot is None:
             slot, clear = self.fslot, self.fslot ^ 1
             self.fslot ^= 1
-            N.check(self.lib.dexmpm_p2g(self._bp, slot, N.ptr(s), None, sp), "dexmpm_p2g")
+            N.check(self.lib.dexmpm_p2g(self._bp, slot, N.ptr(s), None, None, sp), "dexmpm_p2g")
+            tape = None
             N.check(self.lib.dexmpm_grid_op(self._bp, slot, clear, N.ptr(pose), N.ptr(next_pose), sp),
                     "dexmpm_grid_op")
             self.launches += 2
         N.check(self.lib.dexmpm_substep_grad(self._bp, slot, N.ptr(s), N.ptr(s_next), N.ptr(g_next), N.ptr(g),
-                                             N.ptr(pose), N.ptr(next_pose), N.ptr(bgrad), N.ptr(next_bgrad), sp),
+                                             N.ptr(pose), N.ptr(next_pose), N.ptr(bgrad), N.ptr(next_bgrad),
+                                             N.ptr(tape), sp),
                 "dexmpm_substep_grad")
         self.launches += 3
 
@@ -304,10 +309,13 @@ class Rollout:
         nb = max(engine.n_bodies, 1)
         self.poses = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
         self.keep_grids = engine.n_grid_slots >= self.T + 2
+        self.tape = None
         if engine.grad:
             self.ckpt = engine.new_slots(self.S + 1)
             self.ring = engine.new_slots(self.T + 1)
             self.gbuf = engine.new_slots(2)
+            if self.keep_grids:
+                self.tape = engine.new_slots(self.T)
             self.bgrad = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
         else:
             self.ckpt = engine.new_slots(2)
@@ -349,17 +357,20 @@ class Rollout:
         for s in range(T):
             t = k * T + s
             E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1],
-                      slot=(2 + s) if self.keep_grids else None)
+                      slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
             src = self.ring[s + 1]
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):
             t = k * T + s
             cur = self.ckpt[k] if s == 0 else self.ring[s]
             E.substep_grad(cur, self.ring[s + 1], g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
-                           self.bgrad[t + 1], slot=(2 + s) if self.keep_grids else None)
+                           self.bgrad[t + 1], slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
             g_next, g = g, g_next
         if T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])
+
+    def _tape(self, s):
+        return None if self.tape is None else self.tape[s]
 
     def backward_step(self, k: int):
         self._run(self._bwd_graphs, k, self._backward_step)

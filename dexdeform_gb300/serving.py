@@ -89,6 +89,7 @@ class _Batch:
         self.poses = torch.zeros((self.T + 1, nb, 8), device=device)
         if grad:
             self.gbuf = self.E.new_slots(2)
+            self.tape = self.E.new_slots(self.T)
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
         self.use_graphs = use_graphs
         self.graphs = {}
@@ -100,11 +101,11 @@ class _Batch:
     def _backward(self):
         E = self.E
         for s in range(self.T):
-            E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s)
+            E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s, tape=self.tape[s])
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.slot[s], self.slot[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s)
+                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s, tape=self.tape[s])
             g_next, g = g, g_next
         if self.T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])

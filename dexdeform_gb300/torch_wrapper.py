@@ -44,6 +44,7 @@ class DiffSim:
         self.nb = max(self.E.n_bodies, 1)
         self.ring = self.E.new_slots(self.T + 1)
         self.gbuf = self.E.new_slots(2)
+        self.tape = self.E.new_slots(self.T)
         dev = self.E.device
         self.poses = torch.zeros((self.T + 1, self.nb, 8), device=dev)
         self.bgrad = torch.zeros((self.T + 1, self.nb, 8), device=dev)
@@ -59,11 +60,11 @@ class DiffSim:
     def _bwd(self):
         E = self.E
         for s in range(self.T):
-            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s)
+            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s, tape=self.tape[s])
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.ring[s], self.ring[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s)
+                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s, tape=self.tape[s])
             g_next, g = g, g_next
         if self.T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])

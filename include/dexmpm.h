@@ -184,8 +184,10 @@ int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream);
 
 /* P2G into grid slot `slot`: SVD, von Mises, stress, APIC scatter of state
  * slot s; appends the touched blocks to the slot's list.  next_s (nullable)
- * receives the projected F (its 9 F planes). */
-int dexmpm_p2g(const DexBatch *b, int slot, const float *s, float *next_s, dexmpm_stream_t stream);
+ * receives the projected F (its 9 F planes).  tape (nullable): 24 planes of
+ * n_particles floats that receive each particle's SVD of F_tmp (U 0-8, V 9-17,
+ * sigma 18-20, sigma - 1 21-23) for the adjoint of this substep. */
+int dexmpm_p2g(const DexBatch *b, int slot, const float *s, float *next_s, float *tape, dexmpm_stream_t stream);
 
 /* Grid update on the active blocks of `slot`, with body poses at the substep
  * start (pose) and end (next_pose); then clears grid slot clear_slot (< 0: none). */
@@ -197,16 +199,17 @@ int dexmpm_g2p(const DexBatch *b, int slot, const float *s, float *next_s, dexmp
 
 /* One forward substep: dexmpm_p2g + dexmpm_grid_op + dexmpm_g2p. */
 int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *s, float *next_s, const float *pose,
-                   const float *next_pose, dexmpm_stream_t stream);
+                   const float *next_pose, float *tape, dexmpm_stream_t stream);
 
 /* Adjoint of the substep whose forward (p2g + grid_op) filled grid slot
  * `slot` from state s.  next_s is the state after the substep (its v sets the
  * clamp mask), g_next the gradient of next_s, g the gradient of s
  * (overwritten).  Body-pose gradients are added to bgrad / next_bgrad.  The
- * slot is cleared for reuse. */
+ * slot is cleared for reuse.  tape (nullable): the SVD tape the forward P2G of
+ * this substep wrote; without it the adjoint recomputes the SVD. */
 int dexmpm_substep_grad(const DexBatch *b, int slot, const float *s, const float *next_s, const float *g_next,
                         float *g, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
-                        dexmpm_stream_t stream);
+                        const float *tape, dexmpm_stream_t stream);
 
 /* The three kernels of dexmpm_substep_grad, callable one by one: G2P adjoint
  * (writes the x gradient of s, scatters dL/dv_out), grid-update adjoint
@@ -216,7 +219,7 @@ int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *s, const float *ne
                     float *g, dexmpm_stream_t stream);
 int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const float *next_pose, float *bgrad,
                         float *next_bgrad, dexmpm_stream_t stream);
-int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *s, const float *g_next, float *g,
+int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *s, const float *g_next, float *g, const float *tape,
                     dexmpm_stream_t stream);
 
 /* One forward substep (P2G, grid update, G2P) of ONE environment that

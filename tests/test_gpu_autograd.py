@@ -183,3 +183,41 @@ def test_exact_capsule_adjoint_matches_oracle(cuda, oracle_mod):
     b = bg.cpu().numpy()
     assert rel(b[0, :, :3], bp) < 1e-3 and rel(b[0, :, 4:], br) < 1e-3
     assert rel(b[1, :, :3], nbp) < 1e-3 and rel(b[1, :, 4:], nbr) < 1e-3
+
+
+def test_svd_tape_matches_recomputed_svd(cuda):
+    """The recomputed forward P2G stores each particle's SVD of F_tmp (the
+    tape) and the P2G adjoint reads it instead of repeating the SVD: the tape
+    reconstructs F_tmp = (I + dt C) F, and the gradient equals the one that
+    recomputes the SVD (up to the float-atomic ordering of the scatters)."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec
+    env = W.tiny_env(5, n=1024, grid=32, nb=6, steps=1, dt=1e-4)
+    st = W.perturb_state(env, seed=8, v_scale=0.2, c_scale=1.0, f_scale=0.05)
+    E = BatchEngine([EnvSpec.from_env(env)], grad=True, grid_slots=3)
+    s0 = E.pack_state([st])
+    s1, tape, g_next = E.new_slots(3)
+    g_next.copy_(torch.randn_like(g_next))
+    poses = _poses(env, 0, 1)
+    nb = max(E.n_bodies, 1)
+    outs = []
+    for use_tape in (True, False):
+        bg = torch.zeros((2, nb, 8), device="cuda")
+        g = torch.empty_like(s0)
+        E.substep(s0, s1, poses[0], poses[1], slot=2, tape=tape if use_tape else None)
+        E.substep_grad(s0, s1, g_next, g, poses[0], poses[1], bg[0], bg[1], slot=2,
+                       tape=tape if use_tape else None)
+        outs.append((g.clone(), bg.clone()))
+    assert E.error_word() == 0
+    n = env.n
+    T_ = tape[:, :n].double().cpu().numpy()
+    U = T_[0:9].T.reshape(n, 3, 3)
+    V = T_[9:18].T.reshape(n, 3, 3)
+    sig = T_[18:21].T
+    Ft = np.einsum("nij,njk->nik", np.eye(3) + 1e-4 * st["C"].astype(np.float64), st["F"].astype(np.float64))
+    rec = np.einsum("nij,nj,nkj->nik", U, sig, V)
+    assert np.abs(rec - Ft).max() < 1e-5
+    assert np.allclose(T_[21:24].T, sig - 1.0, atol=1e-6)
+    (ga, ba), (gb, bb) = outs
+    assert rel(ga.cpu().numpy(), gb.cpu().numpy()) < 1e-5
+    assert rel(ba.cpu().numpy(), bb.cpu().numpy()) < 1e-4
