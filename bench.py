@@ -361,12 +361,12 @@ def kernel_times(E, R, s0, g_final):
 # Algorithmic bytes per particle (N) and per cell of the active blocks (A)
 # for each kernel: particle state read/written once, grid float4 cells once.
 ALG_BYTES = {
-    "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
+    "p2g": (284, 16),          # x v F C + m vol mu lam yield read, F' + 33-plane tape written; m,mv scattered
     "grid_op": (0, 32),        # (mv, m) read, v_out written (slot kept for the adjoint)
     "g2p": (72, 16),           # x read, x v C written; v_out gathered
     "g2p_grad": (96, 32),      # x, v', dL/d(x v C)' read, dL/dx written; v_out read, dL/dv_out scattered
     "grid_op_grad": (0, 80),   # (mv, m), dL/dv_out read, dL/d(mv, m) written, dL/dv_out and the slot zeroed
-    "p2g_grad": (260, 16),     # x v F C + material + dL/dF', dL/dx read, dL/d(x v F C) written; dL/d(mv,m) gathered
+    "p2g_grad": (392, 16),     # x v F C + material + tape + dL/dF', dL/dx read, dL/d(x v F C) written; dL/d(mv,m) gathered
 }
 
 

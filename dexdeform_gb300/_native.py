@@ -16,6 +16,7 @@ OK, ERR_ARG, ERR_LAUNCH, ERR_OUT_OF_GRID, ERR_TOO_MANY_BODIES = 0, 1, 2, 4, 8
 MAX_BODIES = 32
 FLAG_EXACT_CAPSULE_GRAD = 1
 STATE_PLANES = 24
+TAPE_PLANES = 33  # DEXMPM_TAPE_PLANES: SVD (24) + stress (9) per particle
 PX, PV, PF, PC = 0, 3, 6, 15
 
 

@@ -80,14 +80,18 @@ __device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m
   for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
 }
 
-// SVD tape: the recomputed forward P2G stores each particle's SVD of F_tmp in
-// 24 planes (U 0-8, V 9-17, sigma 18-20, sigma - 1 21-23) so that the P2G
-// adjoint reads it instead of repeating the SVD.
-__device__ __forceinline__ void store_svd(float *T, int N, int p, const SVD3 &sv) {
+// SVD tape: the recomputed forward P2G stores each particle's SVD of F_tmp
+// and its stress in kTapePlanes planes (U 0-8, V 9-17, sigma 18-20,
+// sigma - 1 21-23, P 24-32, before the -dt vol 4 inv_dx^2 scale) so that the
+// P2G adjoint reads them instead of repeating the SVD and return mapping.
+constexpr int kTapePlanes = 33;
+static_assert(kTapePlanes == DEXMPM_TAPE_PLANES, "tape layout");
+__device__ __forceinline__ void store_tape(float *T, int N, int p, const SVD3 &sv, const m33 &P) {
   stm33(T, N, 0, p, sv.U);
   stm33(T, N, 9, p, sv.V);
   stf3(T, N, 18, p, sv.s);
   stf3(T, N, 21, p, sv.d);
+  stm33(T, N, 24, p, P);
 }
 __device__ __forceinline__ SVD3 load_svd(const float *__restrict__ T, int N, int p) {
   SVD3 sv;
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
   Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
   const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
   if (Snext != nullptr && L.live) stm33(Snext, N, PF, p, pl.newF);
-  if (tape != nullptr && L.live) store_svd(tape, N, p, sv);
+  if (tape != nullptr && L.live) store_tape(tape, N, p, sv, pl.P);
 
   const float scale = L.live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
   const m33 A = pl.P * scale + C * m;
@@ -344,7 +348,7 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
   const int n_live = __popc(__ballot_sync(kFull, L.live));
   if (__popc(heads) > kDirectSegs) {
     // nearly one particle per cell: per-lane vector atomics
-#pragma unroll kNodeUnroll
+#pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
@@ -755,18 +759,34 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   make_stencil(x, E.inv_dx, st);
   if (!stencil_in_grid(E, st)) return;
   const f3 v = ldf3(S, N, PV, p);
-  const m33 F = ldm33(S, N, PF, p);
   const m33 C = ldm33(S, N, PC, p);
   const float m = __ldg(B.mass + p), vol = __ldg(B.vol + p);
-  const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
-              ys = __ldg(B.mu_lam_yield + 2 * N + p);
-  const m33 Et = deviation_tmp(F, C, E.dt);
-  const SVD3 sv = kTape ? load_svd(tape, N, p) : svd3_from_deviation(Et);
-  m33 Ft = Et;
-  Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
-  const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
   const float gss = -E.dt * E.inv_dx * vol * 4.f * E.inv_dx;
-  const m33 A = pl.P * gss + C * m;
+  // forward quantities: from the tape, the stress now and the SVD and return
+  // mapping after the gather (fewer values live across its loop); without,
+  // recomputed here
+  m33 F, P;
+  SVD3 sv;
+  Plastic pl;
+  float mu, lam, ys;
+  auto forward_state = [&]() {
+    F = ldm33(S, N, PF, p);
+    mu = __ldg(B.mu_lam_yield + p);
+    lam = __ldg(B.mu_lam_yield + N + p);
+    ys = __ldg(B.mu_lam_yield + 2 * N + p);
+    const m33 Et = deviation_tmp(F, C, E.dt);
+    sv = kTape ? load_svd(tape, N, p) : svd3_from_deviation(Et);
+    m33 Ft = Et;
+    Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
+    pl = constitutive(sv, Ft, mu, lam, ys);
+  };
+  if constexpr (kTape) {
+    P = ldm33(tape, N, 24, p);
+  } else {
+    forward_state();
+    P = pl.P;
+  }
+  const m33 A = P * gss + C * m;
 
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
@@ -805,6 +825,7 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   g_x -= mtv(A, gw);
   const m33 g_stress = Gs * gss, g_C = Gs * m;
   const f3 g_v = gw * m;
+  if constexpr (kTape) forward_state();
 
   // stress -> (U, V, sigma, F_tmp) gradients (integrator.cu:541-625)
   const m33 &nF = pl.newF;

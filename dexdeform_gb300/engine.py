@@ -26,6 +26,7 @@ import torch
 from . import _native as N
 
 SM_COUNT = 152
+TAPE_PLANES = N.TAPE_PLANES
 
 
 @dataclass
@@ -75,8 +76,9 @@ def footprint_bytes(specs: Sequence[EnvSpec], n_slots: int = 2, grad: bool = Fal
     grid_slots = 2 + (substeps if grad else 0)
     b = blocks * 64 * 32 * grid_slots + blocks * 8 * grid_slots + blocks * 4
     b += blocks * 64 * 32 if grad else 0
-    slots = n_slots + ((env_steps + 1) + (substeps + 1) + 2 + substeps if grad else 0)
+    slots = n_slots + ((env_steps + 1) + (substeps + 1) + 2 if grad else 0)
     b += slots * 24 * 4 * n + 5 * 4 * n
+    b += substeps * TAPE_PLANES * 4 * n if grad else 0
     b += (env_steps * substeps + 1) * nb * 32 * (2 if grad else 1)
     return int(b)
 
@@ -195,6 +197,11 @@ class BatchEngine:
     def new_slots(self, n: int) -> torch.Tensor:
         return torch.zeros((n, N.STATE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
 
+    def new_tape(self, n: int) -> torch.Tensor:
+        """n tape slots (the per-particle SVD and stress a recomputed forward
+        P2G stores for its adjoint)."""
+        return torch.zeros((n, TAPE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
+
     def pack_state(self, per_env: Sequence[dict]) -> torch.Tensor:
         """Host dicts (x, v (n,3); F, C (n,3,3)) -> one device slot (24, Np)."""
         buf = np.zeros((N.STATE_PLANES, self.n_particles), np.float32)
@@ -232,8 +239,8 @@ class BatchEngine:
         """One forward substep (P2G, grid update, G2P) of every env.  Without
         `slot` it uses the forward slot pair (alternating, each clearing the
         other); with `slot` (>= 2) it fills that grid slot and keeps it for the
-        adjoint of this substep.  `tape` (a state-shaped slot) receives the
-        SVD of every particle for that adjoint."""
+        adjoint of this substep.  `tape` (a slot of new_tape) receives the SVD
+        and stress of every particle for that adjoint."""
         if slot is None:
             slot, clear = self.fslot, self.fslot ^ 1
             self.fslot ^= 1
@@ -315,7 +322,7 @@ class Rollout:
             self.ring = engine.new_slots(self.T + 1)
             self.gbuf = engine.new_slots(2)
             if self.keep_grids:
-                self.tape = engine.new_slots(self.T)
+                self.tape = engine.new_tape(self.T)
             self.bgrad = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
         else:
             self.ckpt = engine.new_slots(2)

@@ -89,7 +89,7 @@ class _Batch:
         self.poses = torch.zeros((self.T + 1, nb, 8), device=device)
         if grad:
             self.gbuf = self.E.new_slots(2)
-            self.tape = self.E.new_slots(self.T)
+            self.tape = self.E.new_tape(self.T)
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
         self.use_graphs = use_graphs
         self.graphs = {}

@@ -44,7 +44,7 @@ class DiffSim:
         self.nb = max(self.E.n_bodies, 1)
         self.ring = self.E.new_slots(self.T + 1)
         self.gbuf = self.E.new_slots(2)
-        self.tape = self.E.new_slots(self.T)
+        self.tape = self.E.new_tape(self.T)
         dev = self.E.device
         self.poses = torch.zeros((self.T + 1, self.nb, 8), device=dev)
         self.bgrad = torch.zeros((self.T + 1, self.nb, 8), device=dev)

@@ -184,9 +184,11 @@ int dexmpm_reset(const DexBatch *b, dexmpm_stream_t stream);
 
 /* P2G into grid slot `slot`: SVD, von Mises, stress, APIC scatter of state
  * slot s; appends the touched blocks to the slot's list.  next_s (nullable)
- * receives the projected F (its 9 F planes).  tape (nullable): 24 planes of
- * n_particles floats that receive each particle's SVD of F_tmp (U 0-8, V 9-17,
- * sigma 18-20, sigma - 1 21-23) for the adjoint of this substep. */
+ * receives the projected F (its 9 F planes).  tape (nullable): DEXMPM_TAPE_PLANES
+ * planes of n_particles floats that receive each particle's SVD of F_tmp and
+ * stress (U 0-8, V 9-17, sigma 18-20, sigma - 1 21-23, P 24-32 before the
+ * -dt vol 4 inv_dx^2 scale) for the adjoint of this substep. */
+#define DEXMPM_TAPE_PLANES 33
 int dexmpm_p2g(const DexBatch *b, int slot, const float *s, float *next_s, float *tape, dexmpm_stream_t stream);
 
 /* Grid update on the active blocks of `slot`, with body poses at the substep
@@ -205,8 +207,8 @@ int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *s, 
  * `slot` from state s.  next_s is the state after the substep (its v sets the
  * clamp mask), g_next the gradient of next_s, g the gradient of s
  * (overwritten).  Body-pose gradients are added to bgrad / next_bgrad.  The
- * slot is cleared for reuse.  tape (nullable): the SVD tape the forward P2G of
- * this substep wrote; without it the adjoint recomputes the SVD. */
+ * slot is cleared for reuse.  tape (nullable): the tape the forward P2G of this
+ * substep wrote; without it the adjoint recomputes the SVD and return mapping. */
 int dexmpm_substep_grad(const DexBatch *b, int slot, const float *s, const float *next_s, const float *g_next,
                         float *g, const float *pose, const float *next_pose, float *bgrad, float *next_bgrad,
                         const float *tape, dexmpm_stream_t stream);

@@ -196,7 +196,8 @@ def test_svd_tape_matches_recomputed_svd(cuda):
     st = W.perturb_state(env, seed=8, v_scale=0.2, c_scale=1.0, f_scale=0.05)
     E = BatchEngine([EnvSpec.from_env(env)], grad=True, grid_slots=3)
     s0 = E.pack_state([st])
-    s1, tape, g_next = E.new_slots(3)
+    s1, g_next = E.new_slots(2)
+    tape = E.new_tape(1)[0]
     g_next.copy_(torch.randn_like(g_next))
     poses = _poses(env, 0, 1)
     nb = max(E.n_bodies, 1)
