@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--envs", type=int, default=N_ENVS)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
     return ap.parse_args()
 
 
@@ -279,6 +281,10 @@ def run_ours(args, rank, world, local):
 
     plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
     cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs, budget_s=12.0)
+    del R, E
+    torch.cuda.empty_cache()
+    serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank)
+    large = None if (args.no_large or world > 1) else large_env_leg(dev)
 
     if rank == 0:
         ps = sorted(per_step)
@@ -306,6 +312,10 @@ def run_ours(args, rank, world, local):
             out["batched_vs_plain"] = {"fwd": fwd_value / plain["fwd"], "fwd_bwd": value / plain["fwd_bwd"]}
         if cpu is not None:
             out["cpu_baseline"] = cpu
+        if serving is not None:
+            out["serving"] = serving
+        if large is not None:
+            out["large_env"] = large
         out["clocks"] = clk.summary()
         print(json.dumps(out))
 
@@ -384,6 +394,79 @@ def roofline(E, kt, cells):
             "note": "traffic from ncu: see profiles/ (capture on a reduced case, scaled per particle)"}
 
 
+def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
+    """Continuous-batching server on the serving workload: Poisson arrivals,
+    grids 48/64/96^3, particles log-uniform in [2,000, 50,000], horizons
+    uniform in [5, 100] env steps x 50 substeps, 30% gradient requests, HBM
+    admission within 180 GB.  Latency = completion - arrival (queueing
+    included); throughput = particle-substeps served / wall time."""
+    import torch
+    from dexdeform_gb300.serving import Server, latency_stats, poisson_requests
+    reqs = poisson_requests(seed=seed, n=n_req, rate_hz=rate_hz, substeps=SUBSTEPS)
+    base = torch.cuda.memory_allocated(dev)
+    torch.cuda.reset_peak_memory_stats(dev)
+    srv = Server(substeps=SUBSTEPS, hbm_budget_bytes=180 * 2 ** 30, device=dev)
+    t0 = time.perf_counter()
+    done = srv.run(reqs)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    st = latency_stats(done)
+    return {"value": srv.work / wall, "unit": UNIT, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+            "mean_s": st["mean_s"], "requests": len(done), "grad_requests": int(sum(r.grad for r in reqs)),
+            "rate_hz": rate_hz, "wall_s": round(wall, 3), "rounds": srv.rounds,
+            "peak_hbm_gb": round((torch.cuda.max_memory_allocated(dev) - base) / 2 ** 30, 3),
+            "hbm_budget_gb": 180, "what": "Poisson arrivals, 48/64/96^3 grids, 2k-50k particles, horizons 5-100 env "
+                                          "steps x 50 substeps, 30% gradient requests; continuous batching"}
+
+
+def large_env_leg(dev, substeps=100, env_steps=10):
+    """Large single env: 128^3 grid, 300,000 particles in two stacked cubes
+    (yield 40 / 120), 22 capsules + a palm box, 10 env steps x 100 substeps
+    forward+backward with per-env-step checkpoints and substep recomputation.
+    Peak device memory of the run and achieved GB/s per kernel (algorithmic
+    bytes / CUDA-event time)."""
+    import torch
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec, Rollout
+    env = W.large_env(0, steps=substeps * env_steps)
+    base = torch.cuda.memory_allocated(dev)
+    torch.cuda.reset_peak_memory_stats(dev)
+    E = BatchEngine([EnvSpec.from_env(env)], device=dev, grad=True, grid_slots=substeps + 2)
+    R = Rollout(E, substeps=substeps, env_steps=env_steps)
+    R.poses.copy_(torch.from_numpy(E.pack_poses([env.poses[:, :, :3]], [env.poses[:, :, 3:]])))
+    s0 = E.pack_state([env.state()])
+    g = torch.zeros_like(s0)
+    g[0:3] = 1.0 / env.n
+    for _ in range(2):
+        R.forward(s0)
+        R.backward(g)
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 2
+    a.record()
+    for _ in range(reps):
+        R.forward(s0)
+        R.backward(g)
+    b.record()
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    kt, cells = kernel_times(E, R, s0, g)
+    peak = torch.cuda.max_memory_allocated(dev) - base
+    kern = {}
+    for k, us in kt.items():
+        bp, bc = ALG_BYTES[k]
+        kern[k] = {"us": round(us, 2), "GB/s": round((bp * env.n + bc * cells) / (us * 1e-6) / 1e9, 1)}
+    out = {"value": env.n * substeps * env_steps / (ms / 1e3), "unit": UNIT, "ms_per_rollout": round(ms, 2),
+           "particles": env.n, "grid": list(env.grid_dim), "substeps": substeps * env_steps,
+           "peak_hbm_gb": round(peak / 2 ** 30, 3), "active_cells_per_substep": int(cells), "kernels": kern,
+           "error_word": E.error_word(),
+           "what": "128^3, 300k particles (two cubes, yield 40/120), 22 capsules + palm box, 10 x 100 substeps "
+                   "fwd+bwd, per-env-step checkpoints + recompute"}
+    del R, E
+    torch.cuda.empty_cache()
+    return out
+
+
 def plain_rates(envs, dev, sample_every=8):
     """Plain per-env sequential path: the reference's schedule (memsets + per-kernel
     launches, full per-substep state storage) on the reference-compatible
@@ -433,7 +516,7 @@ def cpu_baseline(envs, budget_s=12.0):
     cores = os.cpu_count()
     t0 = time.perf_counter()
     work, done = 0, 0
-    T = 5
+    T = 20
     for env in envs:
         prm = O.SimParams(grid_dim=env.grid_dim, dx=env.dx, dt=env.dt, gravity=env.gravity,
                           ground_friction=env.ground_friction)
