@@ -33,6 +33,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-substeps/s fwd & fwd+bwd, batched vs plain, 1 GB300 @1e-3 tol; p50/p99"
 UNIT = "particle-substeps/s"
 N_ENVS, SUBSTEPS, ENV_STEPS = 64, 50, 10
+SERVING_SUBSTEPS = 50
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -45,6 +46,8 @@ def parse():
     ap.add_argument("--envs", type=int, default=N_ENVS)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--substeps", type=int, default=SUBSTEPS, help="substeps per env step (profiling cases)")
+    ap.add_argument("--env-steps", type=int, default=ENV_STEPS, help="env steps per rollout (profiling cases)")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     return ap.parse_args()
@@ -292,8 +295,9 @@ def run_ours(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.batch_envs)",
-            "config": {"workload": "batch: 64 envs x 64^3 grid, log-uniform 2k-30k particles, 22 capsules/env, "
-                                   "10 env steps x 50 substeps, fwd+bwd with per-env-step checkpoints, CUDA graphs",
+            "config": {"workload": f"batch: {len(envs)} envs x 64^3 grid, log-uniform 2k-30k particles, 22 capsules/env, "
+                                   f"{ENV_STEPS} env steps x {SUBSTEPS} substeps, fwd+bwd with per-env-step "
+                                   "checkpoints, CUDA graphs",
                        "n_envs": len(envs), "particles_per_replica": n_total, "substeps": SUBSTEPS * ENV_STEPS,
                        "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
                        "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1], "source": "autotune"},
@@ -321,9 +325,11 @@ def run_ours(args, rank, world, local):
 
 
 def kernel_times(E, R, s0, g_final):
-    """Average device time (us) of each kernel over one env step (forward
-    recompute keeping its grid slots, then the adjoint), from CUDA events
-    around eager launches on the current stream."""
+    """Average device time (us) of each kernel over one env step, from CUDA
+    events around eager launches on the current stream: the forward pass
+    (alternating grid slots, each grid update clearing the other), the
+    recompute of the backward (P2G writing the tape, grid slots kept), then
+    the adjoint."""
     import torch
     from dexdeform_gb300 import _native as N
     L, sp = E.lib, N.stream_ptr()
@@ -339,12 +345,21 @@ def kernel_times(E, R, s0, g_final):
 
     ring, ck = R.ring, R.ckpt
     src = ck[0]
-    for s in range(T):
+    for s in range(T):  # forward pass
+        slot, clear, dst = E.fslot, E.fslot ^ 1, ring[s + 1]
+        E.fslot ^= 1
+        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), None, sp), "p2g"))
+        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, clear, N.ptr(R.poses[s]),
+                                                          N.ptr(R.poses[s + 1]), sp), "grid_op"))
+        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
+        src = dst
+    src = ck[0]
+    for s in range(T):  # recompute of the backward
         slot, dst = 2 + s, ring[s + 1]
-        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), N.ptr(R._tape(s)), sp),
-                                     "p2g"))
-        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, -1, N.ptr(R.poses[s]), N.ptr(R.poses[s + 1]),
-                                                          sp), "grid_op"))
+        timed("p2g_tape", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), N.ptr(R._tape(s)), sp),
+                                          "p2g"))
+        timed("grid_op_keep", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, -1, N.ptr(R.poses[s]),
+                                                               N.ptr(R.poses[s + 1]), sp), "grid_op"))
         timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
         src = dst
     torch.cuda.synchronize()
@@ -371,8 +386,10 @@ def kernel_times(E, R, s0, g_final):
 # Algorithmic bytes per particle (N) and per cell of the active blocks (A)
 # for each kernel: particle state read/written once, grid float4 cells once.
 ALG_BYTES = {
-    "p2g": (284, 16),          # x v F C + m vol mu lam yield read, F' + 33-plane tape written; m,mv scattered
-    "grid_op": (0, 32),        # (mv, m) read, v_out written (slot kept for the adjoint)
+    "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
+    "p2g_tape": (284, 16),     # as p2g, plus the 33-plane tape written (recompute of the backward)
+    "grid_op": (0, 48),        # (mv, m) read, v_out written, the previous substep's cells cleared
+    "grid_op_keep": (0, 32),   # (mv, m) read, v_out written (slot kept for the adjoint)
     "g2p": (72, 16),           # x read, x v C written; v_out gathered
     "g2p_grad": (96, 32),      # x, v', dL/d(x v C)' read, dL/dx written; v_out read, dL/dv_out scattered
     "grid_op_grad": (0, 80),   # (mv, m), dL/dv_out read, dL/d(mv, m) written, dL/dv_out and the slot zeroed
@@ -380,18 +397,33 @@ ALG_BYTES = {
 }
 
 
+# DRAM bytes (read + write) per particle of one launch, from ncu captures
+# on the 64-env batch (profiles/k_*_batch64.md)
+NCU_DRAM_BYTES_PER_PARTICLE = {"p2g": 84.951296e6 / 654552, "p2g_grad": 239.917568e6 / 654552,
+                               "g2p_grad": 63.15264e6 / 654552}
+
+LAUNCHES_PER_SUBSTEP = {"p2g": 1, "p2g_tape": 1, "grid_op": 1, "grid_op_keep": 1, "g2p": 2, "g2p_grad": 1,
+                        "grid_op_grad": 1, "p2g_grad": 1}
+
+
 def roofline(E, kt, cells):
     import torch
     peak, src = peaks()
-    top = max(kt, key=kt.get)
+    # dominant kernel: largest device time per fwd+bwd substep (G2P runs in
+    # both the forward pass and the recompute)
+    per_substep = {k: v * LAUNCHES_PER_SUBSTEP[k] for k, v in kt.items()}
+    top = max(per_substep, key=per_substep.get)
     n = sum(s.n for s in E.specs)
     bp, bc = ALG_BYTES[top]
     alg = bp * n + bc * cells
     achieved = alg / (kt[top] * 1e-6) / 1e9
     return {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": src, "alg_bytes_per_launch": int(alg),
-            "avg_launch_us": kt[top], "traffic": None,
-            "note": "traffic from ncu: see profiles/ (capture on a reduced case, scaled per particle)"}
+            "avg_launch_us": kt[top],
+            "traffic": int(NCU_DRAM_BYTES_PER_PARTICLE[top] * n) if top in NCU_DRAM_BYTES_PER_PARTICLE else None,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the kernel on the "
+                            "same 64-env batch (654,552 particles, 5 substeps per env step), per particle x n; "
+                            "profiles/<kernel>_batch64.md"}
 
 
 def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
@@ -402,10 +434,10 @@ def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
     included); throughput = particle-substeps served / wall time."""
     import torch
     from dexdeform_gb300.serving import Server, latency_stats, poisson_requests
-    reqs = poisson_requests(seed=seed, n=n_req, rate_hz=rate_hz, substeps=SUBSTEPS)
+    reqs = poisson_requests(seed=seed, n=n_req, rate_hz=rate_hz, substeps=SERVING_SUBSTEPS)
     base = torch.cuda.memory_allocated(dev)
     torch.cuda.reset_peak_memory_stats(dev)
-    srv = Server(substeps=SUBSTEPS, hbm_budget_bytes=180 * 2 ** 30, device=dev)
+    srv = Server(substeps=SERVING_SUBSTEPS, hbm_budget_bytes=180 * 2 ** 30, device=dev)
     t0 = time.perf_counter()
     done = srv.run(reqs)
     torch.cuda.synchronize(dev)
@@ -567,7 +599,9 @@ def run_reference(args, rank, world):
 
 
 def main():
+    global SUBSTEPS, ENV_STEPS
     args = parse()
+    SUBSTEPS, ENV_STEPS = args.substeps, args.env_steps
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         world = int(os.environ.get("WORLD_SIZE", "1"))
