@@ -39,7 +39,7 @@ using namespace dexmpm;
 #define DEX_P2G_GRAD_MINB 4
 #endif
 #ifndef DEX_G2P_GRAD_MINB
-#define DEX_G2P_GRAD_MINB 2
+#define DEX_G2P_GRAD_MINB 3
 #endif
 #ifndef DEX_NODE_UNROLL
 #define DEX_NODE_UNROLL 1
