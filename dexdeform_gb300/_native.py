@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_float, c_int, c_int32, c_void_p
+from ctypes import c_bool, POINTER, c_char_p, c_float, c_int, c_int32, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libdexmpm.so")
@@ -56,6 +56,8 @@ _REF_SIGS = {
     "g2p_grad": [P, P, P, c_float, c_float, c_float, P, P, c_float, P, P, c_int, P, P, P, P, P, P],
     "compute_dist": [P] * 6 + [c_int] + [P] * 4 + [c_int, c_int, P],
     "particle2mass": [P, P, P, P, c_float, c_float, P, P, P, P, c_int, c_int, c_int, P],
+    "particle_sdf": [P] * 5 + [c_int, P, c_float] + [P] * 3 + [c_int, P],
+    "render": [P] * 13 + [c_float, P, c_int, c_bool, P, c_int, c_int, c_float, c_int, P, P],
 }
 _BATCH_SIGS = {
     "dexmpm_reset": [POINTER(DexBatch), P],

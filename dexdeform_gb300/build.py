@@ -17,7 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libdexmpm.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["batched.cu", "ref_abi.cu", "noalloc.cu"]
+SOURCES = ["batched.cu", "ref_abi.cu", "noalloc.cu", "render.cu"]
+# the renderer keeps the reference's unfused float arithmetic (its images are
+# compared pixel by pixel with the reference's code run on the host)
+SOURCE_FLAGS = {"render.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -41,7 +44,7 @@ def build(verbose: bool = False, extra_flags=()) -> str:
     for src in SOURCES:
         obj = os.path.join(tmp, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmds.append([cc, *_flags(extra_flags), "-c", os.path.join(CSRC, src), "-o", obj])
+        cmds.append([cc, *_flags(extra_flags), *SOURCE_FLAGS.get(src, []), "-c", os.path.join(CSRC, src), "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=len(cmds)) as ex:
         for cmd, res in zip(cmds, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds)):
             if res.returncode != 0:

@@ -171,6 +171,7 @@ class MPMSimulator:
         self.particle_mass = DeviceArray((self.n_particles,))
         self.particle_mu_lam_yield = DeviceArray((self.n_particles, 3))
         self.particle_ids = DeviceArray((self.n_particles,), dtype=torch.int32)
+        self.particle_color = DeviceArray((self.n_particles,), dtype=torch.int32)  # 0xRRGGBB per particle
         self.dists = DeviceArray((self.n_particles * max(n_bodies, 1),))
         self.dists_grad = DeviceArray((self.n_particles * max(n_bodies, 1),))
         self.body_type_mu_softness_round = DeviceArray((max(n_bodies, 1), 4))
@@ -220,6 +221,12 @@ class MPMSimulator:
     def get_object_id(self, device):
         assert device == "numpy"
         return self.object_id
+
+    def set_color(self, inp):
+        """Packed 0xRRGGBB colors for the renderer (mpm/simulator.py:263-266)."""
+        color = self.particle_color.download(self.n_particles)
+        color[:] = inp
+        self.particle_color.upload(color)
 
     def set_softness(self, softness):
         pp = self.body_type_mu_softness_round.download()

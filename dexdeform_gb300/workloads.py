@@ -244,3 +244,31 @@ def perturb_state(env: Env, seed=1, v_scale=0.5, c_scale=5.0, f_scale=0.05):
     st["C"] = (rng.normal(size=st["C"].shape) * c_scale).astype(np.float32)
     st["F"] = (np.eye(3) + rng.normal(size=st["F"].shape) * f_scale).astype(np.float32)
     return st
+
+
+def render_scene(seed=0, n=3000, voxel=32, image=(64, 64), inv_dx=64.0, spp=2, max_ray_depth=2, nb=5):
+    """Seeded renderer input: a colored particle cube (packed 0xRRGGBB), nb - 1
+    capsules and a box above it, a camera looking down at it, and the
+    renderer settings (mpm/renderer.py:17-27 defaults where they apply)."""
+    from .renderer import intrinsic, lookat
+    rng = np.random.default_rng(seed)
+    x = (np.array([0.5, 0.15, 0.5]) + rng.uniform(-0.1, 0.1, (n, 3))).astype(np.float32)
+    color = (rng.integers(0, 256, (n, 3)) * np.array([1 << 16, 1 << 8, 1])).sum(1).astype(np.int32)
+    xl = np.floor(x.astype(np.float32) * np.float32(inv_dx) - 6) / np.float32(inv_dx)
+    bbox_min = xl.min(0).astype(np.float32)
+    vox = (voxel,) * 3 if np.isscalar(voxel) else tuple(voxel)
+    bbox_max = (bbox_min + np.asarray(vox, np.float32) / np.float32(inv_dx)).astype(np.float32)
+    tfsr, args = capsules(rng, nb, r_range=(0.02, 0.04), h_range=(0.05, 0.1))
+    tfsr[nb - 1] = (0.0, BODY_FRICTION, SOFTNESS, 0.0)   # a box
+    args[nb - 1] = (0.04, 0.01, 0.03, 0.0)
+    pos = np.stack([rng.uniform(0.42, 0.58, nb), rng.uniform(0.27, 0.33, nb), rng.uniform(0.42, 0.58, nb)], 1)
+    q = rng.normal(size=(nb, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    R, T = lookat((0.5, 0.2, 0.5), 0.5, 0.3, 1.2)
+    return {"x": x, "color": color, "bbox_min": bbox_min, "bbox_max": bbox_max, "voxel": vox, "inv_dx": inv_dx,
+            "bake": 7, "body_pos": pos.astype(np.float32), "body_rot": q.astype(np.float32),
+            "body_tfsr": np.asarray(tfsr, np.float32), "body_args": np.asarray(args, np.float32),
+            "cam_rot": np.asarray(R, np.float32).reshape(9), "cam_pos": np.asarray(T, np.float32),
+            "cam_intr": intrinsic((image[0], image[1], 3)).astype(np.float32).reshape(9), "image": tuple(image),
+            "sdf_threshold": 0.414, "visualize_shape": 1, "max_ray_depth": max_ray_depth, "spp": spp,
+            "ground": 0.03, "seed": seed, "light": np.array([1.0, 1.0, 0.0], np.float32)}

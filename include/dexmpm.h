@@ -26,6 +26,9 @@
 #define DEXMPM_H
 
 #include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -117,6 +120,34 @@ int particle2mass(float *particle_x, float *particle_m, int *grid_lower, const i
  * pointer out; synchronous).  No counterpart in the reference, which has no
  * error reporting (mpm/csrc/common.h:20-34). */
 int dexmpm_abi_get_error(int32_t *out);
+
+/* Renderer (mpm/renderer.py:88-169).  All pointers are device pointers.
+ *
+ * integrator.cu:1911-1933 -- bake a particle volume: splat every particle
+ * into the (2 bake_size)^3 voxels around it with a 64-bit atomicMin of
+ * (quantised distance << 24 | rgb) into `volume` (filled with (1 << 33) - 1 by
+ * the caller), unpack distance / 255 into sdf and rgb / 255 into color
+ * (float[3] per voxel), then two 3^3 box filters of sdf (border voxels 1;
+ * sdf_tmp is scratch).  Voxel (i, j, k) of the x-major grid_dim lies at
+ * bbox_min + (i, j, k) / inv_dx.  Bit-identical to the reference. */
+int particle_sdf(long long *volume, float *particle_x, int *particle_color, float *bbox_min, float *bbox_max,
+                 int bake_size, const int *grid_dim, float inv_dx, float *sdf, float *color, float *sdf_tmp,
+                 int n_particles, dexmpm_stream_t stream);
+
+/* integrator.cu:1862-1905 -- path-traced image (image_dim = rows, cols) of the
+ * ground plane, n_bodies (<= 64) SDF bodies and, when visualize_shape, the
+ * baked volume's sdf_threshold level set: spp jittered samples per pixel,
+ * max_ray_depth diffuse bounces with a shadow ray towards light_direction.
+ * color_buffer receives float[3] per pixel (vignette, exposure 1.5, sqrt),
+ * depth_buffer the distance of the first hit (1e9 for sky), averaged over
+ * the samples.  Random numbers: SplitMix64 of (seed, pixel, draw index) in
+ * (0, 1], drawn in the reference's order, instead of curand XORWOW states
+ * (which the reference allocates on every call). */
+int render(float *sdf_volume, float *box_min, float *box_max, float *color_volume, float *body_pos, float *body_rot,
+           float *body_type_friction_softness_round, float *body_args, float *camera_rot, float *camera_pos,
+           float *camera_intrinsic, float *color_buffer, float *depth_buffer, float sdf_threshold, const int *grid_dim,
+           int n_bodies, bool visualize_shape, const int *image_dim, int max_ray_depth, int spp, float ground_height,
+           int seed, float *light_direction, dexmpm_stream_t stream);
 
 /* ===================================================================== 2 ==
  * Batched path.

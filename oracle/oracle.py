@@ -320,3 +320,62 @@ def set_capsule_grad(mode: str):
     """``"reference"`` (default): the reference's capsule adjoint, which drops
     the capsule-normal term.  ``"exact"``: its true derivative."""
     _load(ORACLE_SO).orc_set_capsule_grad(ctypes.c_int({"reference": 0, "exact": 1}[mode]))
+
+
+# --------------------------------------------------------------- renderer
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _pp(a):
+    return a.ctypes.data_as(_P)
+
+
+def particle_sdf(backend, x, color, bbox_min, bake, gdim, inv_dx):
+    """Volume bake of mpm/csrc/integrator.cu:1911-1933 (bake, unpack, two
+    smoothing passes) on the CPU.  Returns (packed volume int64, sdf, color
+    (n, 3)).  backend "oracle" (render_oracle.c) or "ref" (the reference's own
+    code built for the host)."""
+    x, color, lo = _f32(x), _i32(color), _f32(bbox_min)
+    g = (ctypes.c_int * 3)(*[int(v) for v in gdim])
+    nv = int(np.prod(gdim))
+    vol = np.full(nv, (1 << 33) - 1, np.int64)
+    sdf, tmp = np.zeros(nv, np.float32), np.zeros(nv, np.float32)
+    colv = np.zeros((nv, 3), np.float32)
+    n = int(x.shape[0])
+    if backend == "oracle":
+        L = _load(ORACLE_SO)
+        L.orc_particle_sdf(_pp(vol), _pp(x), _pp(color), _pp(lo), ctypes.c_int(bake), g, ctypes.c_float(inv_dx),
+                           _pp(sdf), _pp(colv), _pp(tmp), ctypes.c_int(n))
+    else:
+        L = _load(REF_SO)
+        hi = _f32(lo + np.asarray(gdim, np.float32) / np.float32(inv_dx))
+        L.particle_sdf(_pp(vol), _pp(x), _pp(color), _pp(lo), _pp(hi), ctypes.c_int(bake), g,
+                       ctypes.c_float(inv_dx), _pp(sdf), _pp(colv), _pp(tmp), ctypes.c_int(n), None)
+    return vol, sdf, colv
+
+
+def render(backend, sc, sdf, colv):
+    """Path-traced image of integrator.cu:1287-1436 on the CPU for a scene
+    dict (workloads.render_scene); returns (color (H, W, 3), depth (H, W))."""
+    H, W = sc["image"]
+    col, dep = np.zeros((H * W, 3), np.float32), np.zeros(H * W, np.float32)
+    arrs = [_f32(sdf), _f32(sc["bbox_min"]), _f32(sc["bbox_max"]), _f32(colv), _f32(sc["body_pos"]),
+            _f32(sc["body_rot"]), _f32(sc["body_tfsr"]), _f32(sc["body_args"]), _f32(sc["cam_rot"]),
+            _f32(sc["cam_pos"]), _f32(sc["cam_intr"])]
+    g = (ctypes.c_int * 3)(*[int(v) for v in sc["voxel"]])
+    im = (ctypes.c_int * 3)(H, W, 3)
+    light = _f32(sc["light"])
+    nb = int(sc["body_pos"].shape[0])
+    args = [*[_pp(a) for a in arrs], _pp(col), _pp(dep), ctypes.c_float(sc["sdf_threshold"]), g, ctypes.c_int(nb)]
+    tail = [ctypes.c_int(int(sc["max_ray_depth"])), ctypes.c_int(int(sc["spp"])), ctypes.c_float(sc["ground"]),
+            ctypes.c_int(int(sc["seed"])), _pp(light)]
+    if backend == "oracle":
+        _load(ORACLE_SO).orc_render(*args, ctypes.c_int(int(sc["visualize_shape"])), im, *tail)
+    else:
+        _load(REF_SO).render(*args, ctypes.c_bool(bool(sc["visualize_shape"])), im, *tail, None)
+    return col.reshape(H, W, 3), dep.reshape(H, W)

@@ -9,7 +9,9 @@
 //   * threadIdx/blockIdx/blockDim are ordinary globals set by a serial loop,
 //   * launch_kernel (common.h:20-25) is redefined as that loop,
 //   * atomicAdd/atomicMin become plain read-modify-writes (one thread at a time),
-//   * curand is replaced by a stub (only the out-of-scope renderer uses it).
+//   * curand is served by the renderer's counter-based generator
+//     (shim/curand_kernel.h), and the render launcher's cudaMalloc/cudaFree of
+//     its generator states by malloc/free.
 // The include path of integrator.cu is passed in by the build recipe
 // (oracle/build_ref_host.sh) through REF_CSRC.
 #define __host__
@@ -62,4 +64,9 @@ static inline double max(double a, float b) { return a > b ? a : (double)b; }
         kernel args;                                                              \
       }                                                                           \
   }
+#include <cstdlib>
+#include <type_traits>
+#define cudaMalloc(ptr, size) \
+  (*(ptr) = (std::remove_reference<decltype(*(ptr))>::type)std::malloc(size), cudaSuccess)
+#define cudaFree(ptr) (std::free(ptr), cudaSuccess)
 #include STR(REF_CSRC/integrator.cu)

@@ -64,3 +64,21 @@ def oracle_sim(O, env, backend="oracle"):
 
 
 gpu = pytest.mark.gpu
+
+
+def render_fixture(name="ref_render_64.npz"):
+    """(scene dict, outputs) of a committed renderer fixture."""
+    z = np.load(os.path.join(GOLDEN, name))
+    sc = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    for k in ("voxel", "image"):
+        sc[k] = tuple(int(v) for v in sc[k])
+    for k in ("inv_dx", "sdf_threshold", "ground"):
+        sc[k] = float(sc[k])
+    for k in ("bake", "visualize_shape", "max_ray_depth", "spp", "seed"):
+        sc[k] = int(sc[k])
+    return sc, {k: z[k] for k in z.files if not k.startswith("in_")}
+
+
+def sha256(a):
+    import hashlib
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), np.uint8)

@@ -3,11 +3,16 @@
 Runs DexDeform's own mpm/csrc/integrator.cu kernels, compiled for the host by
 oracle/build_ref_host.sh (oracle/_ref/libref_host.so), in the reference's
 substep schedule (mpm/simulator.py:561-585) on small seeded inputs, and saves
-inputs and outputs as compressed .npz files.  Needs the reference tree, so it
-runs only where that exists; the fixtures it writes are committed.
+inputs and outputs as compressed .npz files.  The renderer fixture runs the
+reference's particle_sdf and render launchers (integrator.cu:1862-1933) with
+the counter-based generator of oracle/ref_host/shim/curand_kernel.h.  Needs
+the reference tree, so it runs only where that exists; the fixtures it writes
+are committed.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # all fixtures
+    python tests/golden/make_golden.py render     # only ref_render_64.npz
 """
+import hashlib
 import os
 import sys
 
@@ -18,6 +23,7 @@ sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
 from dexdeform_gb300 import workloads as W  # noqa: E402
 from oracle.oracle import Bodies, CpuMPM, Material, SimParams, ref_available  # noqa: E402
+from oracle import oracle as O  # noqa: E402
 
 
 def env_inputs(env):
@@ -60,9 +66,28 @@ def grad_fixture(name, env, seed=7):
     np.savez_compressed(os.path.join(HERE, name), **env_inputs(env), **out)
 
 
+def digest(a):
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), np.uint8)
+
+
+def render_fixture(name="ref_render_64.npz"):
+    """Volume bake + path-traced 64 x 64 image of workloads.render_scene(0):
+    inputs, the image and depth, and SHA-256 digests of the packed volume,
+    sdf and color volume (bit-exact outputs)."""
+    sc = W.render_scene(0)
+    vol, sdf, colv = O.particle_sdf("ref", sc["x"], sc["color"], sc["bbox_min"], sc["bake"], sc["voxel"], sc["inv_dx"])
+    img, dep = O.render("ref", sc, sdf, colv)
+    np.savez_compressed(os.path.join(HERE, name), image=img, depth=dep, volume_sha256=digest(vol),
+                        sdf_sha256=digest(sdf), color_sha256=digest(colv), sdf_sum=np.float64(sdf.sum()),
+                        **{f"in_{k}": np.asarray(v) for k, v in sc.items()})
+
+
 def main():
     if not ref_available():
         sys.exit("oracle/_ref/libref_host.so missing: run oracle/build_ref_host.sh first")
+    render_fixture()
+    if sys.argv[1:] == ["render"]:
+        return
     # forward: rest start (F = I), 20 substeps, capsules in contact
     rollout_fixture("ref_forward_32.npz", W.tiny_env(0, n=256, grid=32, nb=6, steps=20, dt=1e-4), 20,
                     keep=(1, 5, 20))

@@ -168,3 +168,19 @@ def test_block_culling_never_skips_a_touching_body():
     may, touched = H.block_cull(pose, shapes, blk, dx)
     assert not np.any(touched & ~may)
     assert touched.sum() > 1000 and (~may).sum() > 0.3 * n
+
+
+def test_render_launchers_reject_bad_arguments(native_lib):
+    """Argument checks of particle_sdf / render run before any CUDA call."""
+    import ctypes
+    P = None
+    g = (ctypes.c_int * 3)(8, 8, 8)
+    bad = (ctypes.c_int * 3)(0, 8, 8)
+    im = (ctypes.c_int * 3)(4, 4, 3)
+    one = ctypes.c_void_p(1)  # never dereferenced: rejected before use
+    assert native_lib.particle_sdf(P, one, one, one, one, 7, g, 64.0, one, one, one, 10, P) != 0
+    assert native_lib.particle_sdf(one, one, one, one, one, 7, bad, 64.0, one, one, one, 10, P) != 0
+    args = [one] * 13
+    assert native_lib.render(*args, 0.4, g, 65, True, im, 2, 1, 0.0, 0, one, P) != 0   # > 64 bodies
+    assert native_lib.render(*args, 0.4, g, 1, True, im, 2, 0, 0.0, 0, one, P) != 0    # spp 0
+    assert native_lib.render(*args[:11], P, one, 0.4, g, 1, True, im, 2, 1, 0.0, 0, one, P) != 0  # no color buffer

@@ -119,3 +119,17 @@ def test_oracle_loss_hooks_adjoint_by_finite_differences(oracle_mod):
         xm[p, c] -= eps
         fd = ((o.particle2mass(xp) - o.particle2mass(xm)) * gm).sum() / (2 * eps)
         assert abs(fd - gxm[p, c]) < 1e-4 * max(1, abs(fd))
+
+
+def test_render_oracle_matches_reference_fixture(oracle_mod):
+    """The renderer restatement (oracle/render_oracle.c) against the
+    reference's own particle_sdf and render run on the host with the shared
+    counter-based generator: bit-identical volume, image and depth."""
+    from conftest import render_fixture, sha256
+    sc, ref = render_fixture()
+    vol, sdf, colv = oracle_mod.particle_sdf("oracle", sc["x"], sc["color"], sc["bbox_min"], sc["bake"], sc["voxel"],
+                                             sc["inv_dx"])
+    assert (sha256(vol) == ref["volume_sha256"]).all()
+    assert (sha256(sdf) == ref["sdf_sha256"]).all() and (sha256(colv) == ref["color_sha256"]).all()
+    img, dep = oracle_mod.render("oracle", sc, sdf, colv)
+    assert np.array_equal(img, ref["image"]) and np.array_equal(dep, ref["depth"])
