@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--env-steps", type=int, default=ENV_STEPS, help="env steps per rollout (profiling cases)")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-render", action="store_true")
     return ap.parse_args()
 
 
@@ -288,6 +289,7 @@ def run_ours(args, rank, world, local):
     torch.cuda.empty_cache()
     serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank)
     large = None if (args.no_large or world > 1) else large_env_leg(dev)
+    rend = None if (args.no_render or world > 1) else render_leg(dev, cpu=not args.no_cpu)
 
     if rank == 0:
         ps = sorted(per_step)
@@ -320,6 +322,8 @@ def run_ours(args, rank, world, local):
             out["serving"] = serving
         if large is not None:
             out["large_env"] = large
+        if rend is not None:
+            out["render"] = rend
         out["clocks"] = clk.summary()
         print(json.dumps(out))
 
@@ -496,6 +500,55 @@ def large_env_leg(dev, substeps=100, env_steps=10):
                    "fwd+bwd, per-env-step checkpoints + recompute"}
     del R, E
     torch.cuda.empty_cache()
+    return out
+
+
+def render_leg(dev, cpu=True):
+    """Renderer at the reference's defaults (mpm/renderer.py:17-27: 168^3
+    voxels, 512 x 512, spp 3, 2 bounces, bake size 7, inv_dx 150) on a 20,000
+    particle scene: device time of one frame (volume bake + path tracing,
+    CUDA events), and the CPU restatement on a 128 x 128 frame of the same
+    scene (OpenMP, all host cores), both as pixels/s."""
+    import torch
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.renderer import Renderer
+    sc = W.render_scene(0, n=20000, voxel=168, image=(512, 512), inv_dx=150.0, spp=3, max_ray_depth=2)
+    r = Renderer(spp=3, voxel_res=(168, 168, 168), image_res=(512, 512), max_ray_depth=2, inv_dx=150.0)
+    r.setRT(sc["cam_rot"].reshape(3, 3), sc["cam_pos"])
+    x = torch.tensor(sc["x"], device=dev)
+    col = torch.tensor(sc["color"], device=dev)
+    bodies = [torch.tensor(sc[k], device=dev) for k in ("body_pos", "body_rot", "body_tfsr", "body_args")]
+
+    def frame():
+        r.bake(x, col)
+        return r.trace(*bodies, sc["ground"], seed=0)
+
+    frame()
+    torch.cuda.synchronize(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    a.record()
+    for _ in range(reps):
+        r.bake(x, col)
+        r.trace(*bodies, sc["ground"], seed=0)
+    b.record()
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    out = {"ms_per_frame": round(ms, 3), "pixels_per_s": 512 * 512 / (ms / 1e3), "image": [512, 512], "spp": 3,
+           "max_ray_depth": 2, "voxels": [168] * 3, "particles": 20000,
+           "what": "volume bake + path tracing per frame (device time incl. the host copy of the image)"}
+    if cpu:
+        from oracle import oracle as O
+        small = W.render_scene(0, n=20000, voxel=168, image=(128, 128), inv_dx=150.0, spp=3, max_ray_depth=2)
+        t0 = time.perf_counter()
+        _, sdf, colv = O.particle_sdf("oracle", small["x"], small["color"], small["bbox_min"], 7, small["voxel"], 150.0)
+        t1 = time.perf_counter()
+        O.render("oracle", small, sdf, colv)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"pixels_per_s": 128 * 128 / (t2 - t1), "bake_s": round(t1 - t0, 3),
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": "CPU restatement (oracle/render_oracle.c, OpenMP over pixels), 128 x 128 "
+                                         "frame of the same scene; bake single-threaded"}
     return out
 
 
