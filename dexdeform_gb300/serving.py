@@ -118,7 +118,7 @@ class Server:
     """Continuous-batching MPM server on one GPU."""
 
     def __init__(self, substeps=50, hbm_budget_bytes=180 * 2 ** 30, device="cuda", tile_size=128,
-                 use_graphs=True, max_cached_batches=8):
+                 use_graphs=True, max_cached_batches=8, max_inflight_rounds=3):
         self.T = substeps
         self.budget = int(hbm_budget_bytes)
         self.device = torch.device(device)
@@ -135,6 +135,12 @@ class Server:
         self.s_bwd = torch.cuda.Stream(device=self.device)
         self.rounds = 0
         self.work = 0  # particle-substeps processed
+        # rounds queued on the device ahead of the host: each holds an event
+        # and the requests it finished and batches it used (kept alive until
+        # the event has passed, so their memory is not reused under it)
+        self.max_inflight = max(1, int(max_inflight_rounds))
+        self._round_reqs: List[Request] = []
+        self._round_batches: list = []
 
     # ---------------------------------------------------------- admission
     def submit(self, req: Request):
@@ -173,6 +179,7 @@ class Server:
     # -------------------------------------------------------------- round
     def _forward_round(self, reqs):
         b = self._batch(reqs, grad=False)
+        self._round_batches.append(b)
         E = b.E
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
@@ -192,6 +199,7 @@ class Server:
 
     def _backward_round(self, reqs):
         b = self._batch(reqs, grad=True)
+        self._round_batches.append(b)
         E = b.E
         b.gbuf[1].zero_()
         for e, r in enumerate(reqs):
@@ -258,7 +266,8 @@ class Server:
             out["grad_poses"] = res.bgrad
         r.result = out
         r.phase = "done"
-        r._finish_pending = now
+        r._resident = res  # released with the round's event
+        self._round_reqs.append(r)
         self.done.append(r)
         del self.running[r.rid]
         del self.resident[r.rid]
@@ -266,24 +275,44 @@ class Server:
 
     def run(self, requests: List[Request], clock=None, max_rounds=100000):
         """Serve requests (sorted by arrival) on a wall clock starting now;
-        returns the finished requests with latencies in seconds."""
+        returns the finished requests with latencies in seconds.  The host
+        runs up to max_inflight_rounds rounds ahead of the device; a
+        request's completion time is taken when the event recorded after
+        its last round has passed."""
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
+        inflight = collections.deque()
+        stream = torch.cuda.current_stream(self.device)
+
+        def retire(block):
+            while inflight and (block or inflight[0][0].query()):
+                ev, reqs, _ = inflight.popleft()
+                ev.synchronize()
+                t = now()
+                for r in reqs:
+                    r.finished = t
+                    r._resident = None
+                block = False
+
         rounds = 0
         while (pending or self.queue or self.running) and rounds < max_rounds:
             while pending and pending[0].arrival <= now():
                 self.submit(pending.popleft())
+            self._round_reqs, self._round_batches = [], []
             if not self.step(now()):
-                if pending:
+                retire(block=bool(inflight))
+                if pending and not inflight:
                     time.sleep(max(0.0, min(0.005, pending[0].arrival - now())))
                 continue
-            torch.cuda.current_stream(self.device).synchronize()
-            t = now()
-            for r in self.done:
-                if r.finished is None:
-                    r.finished = t
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            inflight.append((ev, self._round_reqs, self._round_batches))
+            retire(block=len(inflight) > self.max_inflight)
+            retire(block=False)
             rounds += 1
+        while inflight:
+            retire(block=True)
         return self.done
 
 
