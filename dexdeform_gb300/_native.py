@@ -61,6 +61,7 @@ _REF_SIGS = {
 }
 _BATCH_SIGS = {
     "dexmpm_reset": [POINTER(DexBatch), P],
+    "dexmpm_clear_slots": [POINTER(DexBatch), c_int, c_int, P],
     "dexmpm_p2g": [POINTER(DexBatch), c_int, P, P, P, P],
     "dexmpm_grid_op": [POINTER(DexBatch), c_int, c_int, P, P, P],
     "dexmpm_g2p": [POINTER(DexBatch), c_int, P, P, P],

@@ -873,6 +873,36 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   stm33(G, N, PC, p, gC_total);
 }
 
+// Zero the grid cells and flags of the listed blocks of slots [first, last)
+// and, by the last CTA to finish (ticket on done_counter), their list counts:
+// a kept slot whose adjoint will not run is made clean for reuse.
+__global__ void __launch_bounds__(256) k_clear_slots(DexBatch B, int first, int last) {
+  const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  const int per_cta = blockDim.x >> 6;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int X = first; X < last; ++X) {
+    const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
+    float4 *grid = reinterpret_cast<float4 *>(slot_grid(B, X));
+    const int32_t *list = slot_list(B, X);
+    uint32_t *flags = slot_flags(B, X);
+    for (int item = blockIdx.x * per_cta + sub; item < cnt; item += gridDim.x * per_cta) {
+      const int blk = list[item];
+      grid[(blk << 6) + cell] = z4;
+      if (cell == 0) flags[blk] = 0u;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned ticket = atomicAdd(B.done_counter, 1u);
+    if (ticket == gridDim.x - 1) {
+      for (int X = first; X < last; ++X) B.block_count[X] = 0;
+      *B.done_counter = 0u;
+      __threadfence();
+    }
+  }
+}
+
 __global__ void k_reset_counts(DexBatch B) {
   for (int k = threadIdx.x; k < B.n_slots; k += blockDim.x) B.block_count[k] = 0;
   if (threadIdx.x == 0) {
@@ -1005,6 +1035,13 @@ int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float
   rc = dexmpm_grid_op_grad(b, slot, pose, next_pose, bgrad, next_bgrad, stream);
   if (rc) return rc;
   return dexmpm_p2g_grad(b, slot, S, Gnext, G, tape, stream);
+}
+
+int dexmpm_clear_slots(const DexBatch *b, int first, int last, dexmpm_stream_t stream) {
+  if (!valid(b) || first < 0 || last > b->n_slots || first > last) return DEXMPM_ERR_ARG;
+  if (first == last) return DEXMPM_OK;
+  k_clear_slots<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, first, last);
+  return check_launch();
 }
 
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {

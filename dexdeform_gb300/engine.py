@@ -275,6 +275,11 @@ class BatchEngine:
                 "dexmpm_substep_grad")
         self.launches += 3
 
+    def clear_slots(self, first: int, last: int):
+        """Make grid slots [first, last) clean (their adjoint will not run)."""
+        N.check(self.lib.dexmpm_clear_slots(self._bp, int(first), int(last), N.stream_ptr()), "dexmpm_clear_slots")
+        self.launches += 1
+
     def retune(self, tile_size: int, grid_ctas: int):
         """Change the particle tile size and the persistent grid-kernel CTA
         count (launch shape only; no buffer changes)."""
@@ -305,8 +310,11 @@ class Rollout:
     checkpoints (grad mode) and substep recomputation in the backward pass.
     When the engine has T + 2 grid slots, the recomputed substeps keep their
     grids and the adjoint reads them; otherwise the adjoint recomputes P2G and
-    the grid update per substep.  Each env step's forward and backward are
-    captured as CUDA graphs on first use and replayed afterwards."""
+    the grid update per substep.  With kept grids, the forward pass runs its
+    last env step the way the backward would recompute it (kept slots, tape),
+    so the backward of that env step needs no recompute.  Each env step's
+    forward and backward are captured as CUDA graphs on first use and
+    replayed afterwards."""
 
     def __init__(self, engine: BatchEngine, substeps: int, env_steps: int, use_graphs: bool = True):
         self.E = engine
@@ -328,6 +336,7 @@ class Rollout:
             self.ckpt = engine.new_slots(2)
             self.ring = engine.new_slots(2)
         self._fwd_graphs, self._bwd_graphs = {}, {}
+        self._kept_live = False  # slots 2..T+1 and the tape hold the last env step's forward
 
     # ------------------------------------------------------------- forward
     def _ckpt(self, k):
@@ -343,34 +352,60 @@ class Rollout:
             E.substep(src, dst, self.poses[t], self.poses[t + 1])
             src = dst
 
-    def forward_step(self, k: int):
-        self._run(self._fwd_graphs, k, self._forward_step)
-
-    def forward(self, state0: Optional[torch.Tensor] = None):
-        if state0 is not None:
-            self._ckpt(0).copy_(state0)
-        for k in range(self.S):
-            self.forward_step(k)
-        return self._ckpt(self.S)
-
-    # ------------------------------------------------------------ backward
-    def _backward_step(self, k: int):
-        """Gradient of ckpt[k] from the gradient of ckpt[k+1] (in gbuf[1]):
-        recompute the T states of env step k into the ring (keeping each
-        substep's grid slot when there are enough slots), then run the adjoint
-        substeps in reverse.  Result in gbuf[1]."""
+    def _forward_step_kept(self, k: int):
+        """Env step k as the backward recomputes it: states into the ring,
+        grids kept in slots 2..T+1, the tape written; result in ckpt[k+1]."""
         T, E = self.T, self.E
         src = self.ckpt[k]
         for s in range(T):
             t = k * T + s
-            E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1],
-                      slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
-            src = self.ring[s + 1]
+            dst = self.ckpt[k + 1] if s == T - 1 else self.ring[s + 1]
+            E.substep(src, dst, self.poses[t], self.poses[t + 1], slot=2 + s, tape=self._tape(s))
+            src = dst
+
+    def forward_step(self, k: int):
+        self._run(self._fwd_graphs, k, self._forward_step)
+
+    def forward(self, state0: Optional[torch.Tensor] = None, keep_last: bool = True):
+        """Run the S env steps from ckpt[0] (or state0).  keep_last (gradient
+        engines with kept grids): run the last env step as the backward would
+        recompute it, for a backward that follows; pass False for forward-only
+        use."""
+        if state0 is not None:
+            self._ckpt(0).copy_(state0)
+        keep = keep_last and self.E.grad and self.keep_grids and self.S > 0
+        if self._kept_live:
+            self.E.clear_slots(2, 2 + self.T)  # a kept forward whose backward was not taken
+            self._kept_live = False
+        for k in range(self.S - 1 if keep else self.S):
+            self.forward_step(k)
+        if keep:
+            k = self.S - 1
+            run_graph(self.E, self._fwd_graphs, ("kept", k), lambda: self._forward_step_kept(k), self.use_graphs)
+            self._kept_live = True
+        return self._ckpt(self.S)
+
+    # ------------------------------------------------------------ backward
+    def _backward_step(self, k: int, recompute: bool = True):
+        """Gradient of ckpt[k] from the gradient of ckpt[k+1] (in gbuf[1]):
+        recompute the T states of env step k into the ring (keeping each
+        substep's grid slot when there are enough slots) unless the forward
+        kept them, then run the adjoint substeps in reverse.  Result in
+        gbuf[1]."""
+        T, E = self.T, self.E
+        if recompute:
+            src = self.ckpt[k]
+            for s in range(T):
+                t = k * T + s
+                E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1],
+                          slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
+                src = self.ring[s + 1]
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):
             t = k * T + s
             cur = self.ckpt[k] if s == 0 else self.ring[s]
-            E.substep_grad(cur, self.ring[s + 1], g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
+            nxt = self.ckpt[k + 1] if s == T - 1 else self.ring[s + 1]
+            E.substep_grad(cur, nxt, g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
                            self.bgrad[t + 1], slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
             g_next, g = g, g_next
         if T % 2 == 1:
@@ -380,7 +415,15 @@ class Rollout:
         return None if self.tape is None else self.tape[s]
 
     def backward_step(self, k: int):
-        self._run(self._bwd_graphs, k, self._backward_step)
+        if self._kept_live and k == self.S - 1:
+            run_graph(self.E, self._bwd_graphs, ("kept", k), lambda: self._backward_step(k, recompute=False),
+                      self.use_graphs)
+            self._kept_live = False  # the adjoint cleared the kept slots
+        else:
+            if self._kept_live:
+                self.E.clear_slots(2, 2 + self.T)
+                self._kept_live = False
+            self._run(self._bwd_graphs, k, self._backward_step)
 
     def backward(self, g_final: torch.Tensor, on_boundary=None):
         """Back-propagate g_final (gradient of the last checkpoint).

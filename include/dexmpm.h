@@ -255,6 +255,11 @@ int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const fl
 int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *s, const float *g_next, float *g, const float *tape,
                     dexmpm_stream_t stream);
 
+/* Clear grid slots [first, last) whose adjoint will not run (their listed
+ * blocks, flags and list counts), e.g. substeps kept for an adjoint that was
+ * not taken.  No counterpart in the reference. */
+int dexmpm_clear_slots(const DexBatch *b, int first, int last, dexmpm_stream_t stream);
+
 /* One forward substep (P2G, grid update, G2P) of ONE environment that
  * allocates no device memory: for callers that cannot call cudaMalloc, such
  * as a host application whose own pool allocator owns the device memory, or
