@@ -73,24 +73,32 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _all_reduce(x, world, op):
+    """Reduce one scalar over the ranks: NCCL on the GPU (the benchmark),
+    gloo on the CPU (the multi-process tests)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=getattr(dist.ReduceOp, op))
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    return _all_reduce(x, world, "MAX")
 
 
 def sum_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _all_reduce(x, world, "SUM")
+
+
+def weak_scaling_value(work, t_ms, steps, world):
+    """Whole-job particle-substeps/s: the units all ranks processed over the
+    slowest rank's time (each rank runs its own replica batch)."""
+    t_max = max_over_ranks(t_ms, world)
+    return sum_over_ranks(float(work), world) * steps / (t_max / 1e3), t_max
 
 
 class ClockSampler:
@@ -227,9 +235,8 @@ def run_ours(args, rank, world, local):
     gpu_launches = E.launches - launches0
     per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     t_ms = ev[0].elapsed_time(ev[-1])
-    t_ms_max = max_over_ranks(t_ms, world)
+    value, t_ms_max = weak_scaling_value(work, t_ms, args.steps, world)
     work_all = sum_over_ranks(float(work), world)
-    value = work_all * args.steps / (t_ms_max / 1e3)
     # ----- forward only
     for _ in range(3):
         fwd_step()

@@ -921,6 +921,29 @@ bool valid(const DexBatch *b) {
 }
 bool slot_ok(const DexBatch *b, int k) { return k >= 0 && k < b->n_slots; }
 
+// CTAs of a 256-thread grid kernel resident on the whole device at once
+// (occupancy x SM count, cached per device): the persistent grid kernels
+// launch at most that many, so that they run in one wave.
+enum { kGridOp = 0, kGridOpGrad = 1, kClearSlots = 2, kGridKernels = 3 };
+int resident_ctas(const void *kernel, int id) {
+  static std::atomic<int> cache[64][kGridKernels];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  int c = cache[dev][id].load(std::memory_order_relaxed);
+  if (c == 0) {
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    c = per_sm * sms;
+    cache[dev][id].store(c, std::memory_order_relaxed);
+  }
+  return c;
+}
+int grid_ctas(const DexBatch *b, const void *kernel, int id) {
+  const int r = resident_ctas(kernel, id);
+  return b->grid_ctas < r ? b->grid_ctas : r;
+}
+
 // Dynamic shared memory of the scatter kernels for CTAs of `threads`.
 size_t scatter_smem(int threads) { return DEX_SCATTER ? (size_t)(threads / 32) * kScatterSmemPerWarp : 0; }
 
@@ -974,8 +997,8 @@ int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pos
   if (!valid(b) || !slot_ok(b, slot) || (clear_slot >= 0 && (!slot_ok(b, clear_slot) || clear_slot == slot)))
     return DEXMPM_ERR_ARG;
   if (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape)) return DEXMPM_ERR_ARG;
-  k_grid_op<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, slot, clear_slot < 0 ? -1 : clear_slot, pose,
-                                                            next_pose);
+  k_grid_op<<<grid_ctas(b, (const void *)k_grid_op, kGridOp), 256, 0, (cudaStream_t)stream>>>(
+      *b, slot, clear_slot < 0 ? -1 : clear_slot, pose, next_pose);
   return check_launch();
 }
 
@@ -1009,7 +1032,8 @@ int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const fl
                         float *next_bgrad, dexmpm_stream_t stream) {
   if (!grad_ok(b) || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape)) return DEXMPM_ERR_ARG;
-  k_grid_op_grad<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, slot, pose, next_pose, bgrad, next_bgrad);
+  k_grid_op_grad<<<grid_ctas(b, (const void *)k_grid_op_grad, kGridOpGrad), 256, 0, (cudaStream_t)stream>>>(
+      *b, slot, pose, next_pose, bgrad, next_bgrad);
   return check_launch();
 }
 
@@ -1040,7 +1064,8 @@ int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float
 int dexmpm_clear_slots(const DexBatch *b, int first, int last, dexmpm_stream_t stream) {
   if (!valid(b) || first < 0 || last > b->n_slots || first > last) return DEXMPM_ERR_ARG;
   if (first == last) return DEXMPM_OK;
-  k_clear_slots<<<b->grid_ctas, 256, 0, (cudaStream_t)stream>>>(*b, first, last);
+  k_clear_slots<<<grid_ctas(b, (const void *)k_clear_slots, kClearSlots), 256, 0, (cudaStream_t)stream>>>(*b, first,
+                                                                                                   last);
   return check_launch();
 }
 
