@@ -354,24 +354,34 @@ def kernel_times(E, R, s0, g_final):
         acc.setdefault(name, []).append((a, b))
 
     ring, ck = R.ring, R.ckpt
-    src = ck[0]
-    for s in range(T):  # forward pass
-        slot, clear, dst = E.fslot, E.fslot ^ 1, ring[s + 1]
-        E.fslot ^= 1
-        timed("p2g", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), None, sp), "p2g"))
-        timed("grid_op", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, clear, N.ptr(R.poses[s]),
-                                                          N.ptr(R.poses[s + 1]), sp), "grid_op"))
-        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
-        src = dst
-    src = ck[0]
-    for s in range(T):  # recompute of the backward
-        slot, dst = 2 + s, ring[s + 1]
-        timed("p2g_tape", lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(src), N.ptr(dst), N.ptr(R._tape(s)), sp),
-                                          "p2g"))
-        timed("grid_op_keep", lambda: N.check(L.dexmpm_grid_op(E._bp, slot, -1, N.ptr(R.poses[s]),
-                                                               N.ptr(R.poses[s + 1]), sp), "grid_op"))
-        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(src), N.ptr(dst), sp), "g2p"))
-        src = dst
+
+    def pass_(sts, kept):
+        """One env step of the fused sequence: P2G, grid update, then T - 1 x
+        (G2P fused with the next P2G, grid update), then G2P."""
+        def take(t):
+            if kept:
+                return 2 + t, -1
+            slot = E.fslot
+            E.fslot ^= 1
+            return slot, slot ^ 1
+        sfx = "_tape" if kept else ""
+        gname = "grid_op_keep" if kept else "grid_op"
+        slot, clear = take(0)
+        tp = (lambda t: N.ptr(R._tape(t))) if kept else (lambda t: None)
+        timed("p2g" + sfx, lambda: N.check(L.dexmpm_p2g(E._bp, slot, N.ptr(sts[0]), N.ptr(sts[1]), tp(0), sp), "p2g"))
+        timed(gname, lambda: N.check(L.dexmpm_grid_op(E._bp, slot, clear, N.ptr(R.poses[0]), N.ptr(R.poses[1]), sp),
+                                     "grid_op"))
+        for t in range(T - 1):
+            nslot, clear = take(t + 1)
+            timed("g2p2g" + sfx, lambda: N.check(L.dexmpm_g2p2g(E._bp, slot, nslot, N.ptr(sts[t]), N.ptr(sts[t + 1]),
+                                                                N.ptr(sts[t + 2]), tp(t + 1), sp), "g2p2g"))
+            timed(gname, lambda: N.check(L.dexmpm_grid_op(E._bp, nslot, clear, N.ptr(R.poses[t + 1]),
+                                                          N.ptr(R.poses[t + 2]), sp), "grid_op"))
+            slot = nslot
+        timed("g2p", lambda: N.check(L.dexmpm_g2p(E._bp, slot, N.ptr(sts[T - 1]), N.ptr(sts[T]), sp), "g2p"))
+
+    pass_([ck[0]] + [ring[t] for t in range(1, T + 1)], kept=False)   # forward pass
+    pass_([ck[0]] + [ring[t] for t in range(1, T + 1)], kept=True)    # recompute of the backward
     torch.cuda.synchronize()
     cells = float(E.block_count[2:2 + T].double().mean()) * 64  # active cells per substep
     gn, g = R.gbuf[1], R.gbuf[0]
@@ -398,6 +408,8 @@ def kernel_times(E, R, s0, g_final):
 ALG_BYTES = {
     "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
     "p2g_tape": (284, 16),     # as p2g, plus the 33-plane tape written (recompute of the backward)
+    "g2p2g": (164, 32),        # x, F + material read, x v C and F' written; v_out gathered, m,mv scattered
+    "g2p2g_tape": (296, 32),   # as g2p2g, plus the tape written
     "grid_op": (0, 48),        # (mv, m) read, v_out written, the previous substep's cells cleared
     "grid_op_keep": (0, 32),   # (mv, m) read, v_out written (slot kept for the adjoint)
     "g2p": (72, 16),           # x read, x v C written; v_out gathered
@@ -412,8 +424,11 @@ ALG_BYTES = {
 NCU_DRAM_BYTES_PER_PARTICLE = {"p2g": 84.951296e6 / 654552, "p2g_grad": 239.917568e6 / 654552,
                                "g2p_grad": 63.15264e6 / 654552}
 
-LAUNCHES_PER_SUBSTEP = {"p2g": 1, "p2g_tape": 1, "grid_op": 1, "grid_op_keep": 1, "g2p": 2, "g2p_grad": 1,
-                        "grid_op_grad": 1, "p2g_grad": 1}
+# launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
+# P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
+def launches_per_substep(T):
+    return {"p2g": 1 / T, "p2g_tape": 1 / T, "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1,
+            "grid_op_keep": 1, "g2p": 2 / T, "g2p_grad": 1, "grid_op_grad": 1, "p2g_grad": 1}
 
 
 def roofline(E, kt, cells):
@@ -421,7 +436,8 @@ def roofline(E, kt, cells):
     peak, src = peaks()
     # dominant kernel: largest device time per fwd+bwd substep (G2P runs in
     # both the forward pass and the recompute)
-    per_substep = {k: v * LAUNCHES_PER_SUBSTEP[k] for k, v in kt.items()}
+    w = launches_per_substep(SUBSTEPS)
+    per_substep = {k: v * w[k] for k, v in kt.items()}
     top = max(per_substep, key=per_substep.get)
     n = sum(s.n for s in E.specs)
     bp, bc = ALG_BYTES[top]

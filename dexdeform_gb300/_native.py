@@ -65,6 +65,7 @@ _BATCH_SIGS = {
     "dexmpm_p2g": [POINTER(DexBatch), c_int, P, P, P, P],
     "dexmpm_grid_op": [POINTER(DexBatch), c_int, c_int, P, P, P],
     "dexmpm_g2p": [POINTER(DexBatch), c_int, P, P, P],
+    "dexmpm_g2p2g": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P],
     "dexmpm_substep": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P, P],
     "dexmpm_substep_grad": [POINTER(DexBatch), c_int, P, P, P, P, P, P, P, P, P, P],
     "dexmpm_g2p_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],

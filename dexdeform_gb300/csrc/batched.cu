@@ -1,20 +1,23 @@
 // batched.cu -- the batched MLS-MPM substep and its adjoint for sm_103a.
 //
 // Work decomposition (one launch per phase for all environments):
-//   * particle phases (P2G, G2P, their adjoints): one CTA per tile of
-//     `tile_size` particles of one env (tiles never straddle envs);
-//   * grid phases (grid update and its adjoint): a persistent grid of
-//     `grid_ctas` CTAs walking the active-block list, 64 threads per block.
-// Scatters (P2G and the G2P adjoint) pre-reduce in the warp: lanes are sorted
-// by stencil base cell (a 32-wide bitonic sort on shuffles), equal keys form
-// contiguous segments, each of the 27 node contributions is summed over its
-// segment with five shuffle rounds and the segment head issues one float4
-// vector atomic (red.global.add.v4.f32).  Grid storage is an array of slots
-// (mass/momentum grid, post-update velocities, active-block list per slot):
-// forward substeps alternate two slots and each grid update clears the slot
-// the previous substep used; the adjoint of an env step reads the slots its
-// recomputed substeps left behind and clears each one after use, so nothing
-// is recomputed in the backward and nothing is memset per substep.
+//   * particle phases (P2G, G2P, their adjoints, and G2P fused with the next
+//     substep's P2G): one CTA per tile of `tile_size` particles of one env
+//     (tiles never straddle envs);
+//   * grid phases (grid update and its adjoint): a persistent grid of at most
+//     the resident number of CTAs walking the active-block list, 64 threads
+//     per block.
+// Scatters (P2G and the G2P adjoint) pre-reduce in the warp: the warp orders
+// its lanes by stencil base cell (bitonic sort on shuffles), equal bases form
+// segments, and each segment's 27 node sums are formed through a transposed
+// shared-memory buffer and added with one 8-byte vector atomic per node and
+// component pair.  Grid storage is an array of slots (mass/momentum grid,
+// post-update velocities, active-block list per slot): forward substeps
+// alternate two slots and each grid update clears the slot the previous
+// substep used; the adjoint of an env step reads the slots its recomputed
+// substeps left behind (and the tape of their SVDs and stresses) and clears
+// each one after use, so nothing is recomputed inside the adjoint and nothing
+// is memset per substep.
 //
 // Arithmetic follows mpm/csrc/integrator.cu (kernels cited per function); the
 // SVD and stress use the cancellation-free forms of mpm_math.cuh.
@@ -30,13 +33,24 @@ using namespace dexmpm;
 
 // Compile-time tuning knobs.  Defaults were picked by timing every kernel on
 // GB300 over the 64-env batch: minimum resident CTAs per SM (register caps:
-// P2G 85, G2P adjoint 128, P2G adjoint 128 with a few spills) and a rolled
-// outer loop over the 27 stencil nodes (smaller code, fewer live registers).
+// P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint 128) and the unrolling
+// of the outer loop over the 27 stencil nodes (rolled where registers are
+// tight; fully unrolled in the fused kernel's gather and the G2P adjoint's
+// direct scatter, which keeps their weight arrays out of local memory).
 #ifndef DEX_P2G_MINB
 #define DEX_P2G_MINB 3
 #endif
 #ifndef DEX_P2G_GRAD_MINB
 #define DEX_P2G_GRAD_MINB 4
+#endif
+#ifndef DEX_G2P2G_MINB
+#define DEX_G2P2G_MINB 3
+#endif
+#ifndef DEX_G2P_GRAD_UNROLL
+#define DEX_G2P_GRAD_UNROLL 3
+#endif
+#ifndef DEX_G2P2G_UNROLL
+#define DEX_G2P2G_UNROLL 3
 #endif
 #ifndef DEX_G2P_GRAD_MINB
 #define DEX_G2P_GRAD_MINB 3
@@ -44,15 +58,14 @@ using namespace dexmpm;
 #ifndef DEX_NODE_UNROLL
 #define DEX_NODE_UNROLL 1
 #endif
-// Scatter reduction: 1 = transposed through shared memory, 0 = segmented
-// shuffles; warps with more than DEX_DIRECT_SEGS segments use plain atomics.
-#ifndef DEX_SCATTER
-#define DEX_SCATTER 1
-#endif
+// Scatter: warps with more than DEX_DIRECT_SEGS segments of equal stencil
+// base use per-lane atomics instead of the transposed reduction.
 #ifndef DEX_DIRECT_SEGS
 #define DEX_DIRECT_SEGS 8
 #endif
 constexpr int kNodeUnroll = DEX_NODE_UNROLL;
+constexpr int kG2p2gUnroll = DEX_G2P2G_UNROLL;
+constexpr int kG2pGradUnroll = DEX_G2P_GRAD_UNROLL;
 
 namespace {
 
@@ -151,17 +164,6 @@ __device__ __forceinline__ void warp_sort(int &key, int &idx, int lane) {
   }
 }
 
-#if !DEX_SCATTER
-// Suffix sum within contiguous segments; the segment head ends with the total.
-__device__ __forceinline__ float seg_sum(float v, int lane, int seg_end) {
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    float t = __shfl_down_sync(kFull, v, off);
-    if (lane + off <= seg_end) v += t;
-  }
-  return v;
-}
-#endif
 
 __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, float d) {
   atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
@@ -175,16 +177,20 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 // ------------------------------------------------ transposed warp scatter
 // The scatter kernels add 27 node contributions per particle to the grid.
-// Lanes are sorted by stencil base, so equal bases (same 27 target cells) are
-// contiguous segments.  Per group of up to 16 nodes every lane stores its
-// float4 per node in a per-warp shared buffer; then lane l owns component pair
-// (l & 1) of node (l >> 1), sums it over each segment with plain loads, and
-// the segment's total goes to the grid in one 8-byte vector atomic.  Rows are
+// Every lane keeps its own particle; the warp orders its lanes by (stencil
+// base, lane) with a 32-wide bitonic sort on shuffles, so that equal bases
+// (the same 27 target cells) form contiguous segments of positions.  Per group
+// of up to 16 nodes every lane stores its float4 per node at its position's
+// column of a per-warp shared buffer; then lane l owns component pair (l & 1)
+// of node (l >> 1), sums it over each segment with plain loads, and the
+// segment's total goes to the grid in one 8-byte vector atomic.  Rows are
 // padded to 132 floats so that both the stores (16 B per lane) and the loads
-// (8 B per lane, one row per lane pair) are free of bank conflicts.
-constexpr int kRedRow = 132;                 // floats per node row (32 lanes x 4 + 4 pad)
-constexpr int kRedWarpFloats = 16 * kRedRow;  // 16 node rows per warp
-constexpr int kDirectSegs = DEX_DIRECT_SEGS;  // more segments than this: per-lane atomics instead
+// (8 B per lane, one row per lane pair) are free of bank conflicts.  Warps
+// with more than DEX_DIRECT_SEGS segments (about one particle per cell) add
+// their contributions with per-lane float4 atomics instead.
+constexpr int kRedRow = 132;                      // floats per node row (32 lanes x 4 + 4 pad)
+constexpr int kRedWarpFloats = 16 * kRedRow + 32;  // 16 node rows + the position table
+constexpr int kDirectSegs = DEX_DIRECT_SEGS;
 constexpr size_t kScatterSmemPerWarp = sizeof(float) * kRedWarpFloats;
 
 __device__ __forceinline__ float *warp_red_buffer() {
@@ -192,28 +198,55 @@ __device__ __forceinline__ float *warp_red_buffer() {
   return reinterpret_cast<float *>(s_dyn) + (threadIdx.x >> 5) * kRedWarpFloats;
 }
 
-__device__ __forceinline__ void red_put(float *red, int c, int lane, float a, float b, float d, float e) {
-  *reinterpret_cast<float4 *>(red + c * kRedRow + 4 * lane) = make_float4(a, b, d, e);
+// This lane's position in the warp's (key, lane) order and the segment
+// structure of that order (key INT_MAX: no contribution, sorts last).
+struct Ranked {
+  int r;           // position of this lane
+  int src;         // lane at position `lane` (for per-segment lookups)
+  unsigned heads;  // bit q: position q starts a segment of live lanes
+  int n_live;      // live lanes occupy positions [0, n_live)
+  bool head;       // this lane starts its segment
+};
+__device__ __forceinline__ Ranked rank_lanes(int key, int lane, float *red) {
+  int k = key, src = lane;
+  warp_sort(k, src, lane);  // lane q now holds position q
+  int *pos = reinterpret_cast<int *>(red + 16 * kRedRow);
+  pos[src] = lane;
+  __syncwarp();
+  Ranked R;
+  R.r = pos[lane];
+  R.src = src;
+  const int prev = __shfl_up_sync(kFull, k, 1);
+  R.heads = __ballot_sync(kFull, k != INT_MAX && (lane == 0 || prev != k));
+  R.n_live = __popc(__ballot_sync(kFull, k != INT_MAX));
+  R.head = (R.heads >> R.r) & 1u;
+  __syncwarp();
+  return R;
+}
+
+__device__ __forceinline__ void red_put(float *red, int c, int pos, float a, float b, float d, float e) {
+  *reinterpret_cast<float4 *>(red + c * kRedRow + 4 * pos) = make_float4(a, b, d, e);
 }
 
 // Sum the stored rows of nodes node0 .. node0 + n_nodes - 1 over every segment
-// (heads: lanes starting a segment; n_live: live lanes, which come first) and
-// add them at the segment's stencil base + node offset.  Warp-uniform.
-__device__ __forceinline__ void red_walk(const float *red, unsigned heads, int n_live, int node0, int n_nodes,
-                                         const int base[3], const DexEnv &E, float *grid, int lane) {
+// of positions and add them at the segment's stencil base + node offset (base:
+// each lane's own particle's base).  Warp-uniform.
+__device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int node0, int n_nodes, const int base[3],
+                                         const DexEnv &E, float *grid, int lane) {
   const int c = lane >> 1, h = lane & 1;
   const int n = node0 + c;
   const bool act = c < n_nodes;
   const int ni = n / 9, nj = (n / 3) % 3, nk = n % 3;
   const float *col = red + c * kRedRow + 2 * h;
-  unsigned rest = heads;
+  unsigned rest = R.heads;
   while (rest) {
     const int start = __ffs(rest) - 1;
     rest &= rest - 1u;
-    const int end = rest ? __ffs(rest) - 1 : n_live;
-    const int bx = __shfl_sync(kFull, base[0], start);
-    const int by = __shfl_sync(kFull, base[1], start);
-    const int bz = __shfl_sync(kFull, base[2], start);
+    const int end = rest ? __ffs(rest) - 1 : R.n_live;
+    const int owner = __shfl_sync(kFull, R.src, start);
+    const int bx = __shfl_sync(kFull, base[0], owner);
+    const int by = __shfl_sync(kFull, base[1], owner);
+    const int bz = __shfl_sync(kFull, base[2], owner);
     float2 acc = make_float2(0.f, 0.f);
     for (int q = start; q < end; ++q) {
       const float2 t = *reinterpret_cast<const float2 *>(col + 4 * q);
@@ -269,84 +302,48 @@ __device__ __forceinline__ uint32_t bodies_near_block(const DexBatch &B, const D
   return __ballot_sync(kFull, near);
 }
 
-// Per-lane particle selection shared by the scatter kernels: lanes are sorted
-// by stencil base so that equal cells are contiguous.  Returns the particle
-// index (valid even when !live) and fills the segment info.
-struct Lane {
-  int p;
-  bool live, head, lone;
-  int seg_end;
-};
-
-__device__ __forceinline__ Lane sorted_lane(const DexBatch &B, const DexEnv &E, const float *__restrict__ S,
-                                            int first) {
+// =================================================================== P2G
+// integrator.cu:84-100 (compute_svd) fused with :312-394 (p2g) for the
+// particle of this lane: SVD of F_tmp = (I + dt C) F, return mapping, the
+// projected F (to Fout's F planes), the tape, and the APIC momentum + stress
+// scatter into grid slot X, marking the blocks the stencil touches.  `live`
+// lanes contribute; every lane of the warp calls it.
+__device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int X, int p, bool live, f3 x, f3 v,
+                                         const m33 &F, const m33 &C, float *Fout, float *tape, int lane) {
   const int N = B.n_particles;
-  const int lane = threadIdx.x & 31;
-  const int wfirst = first + (threadIdx.x & ~31);
-  int loc = first + threadIdx.x;
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
   int key = INT_MAX;
-  if (loc < E.n) {
-    Stencil st;
-    make_stencil(ldf3(S, N, PX, E.p_off + loc), E.inv_dx, st);
+  if (live) {
     if (stencil_in_grid(E, st)) {
       key = (st.base[0] * E.gy + st.base[1]) * E.gz + st.base[2];
     } else {
       atomicOr(B.error, DEXMPM_ERR_OUT_OF_GRID);
+      live = false;
     }
   }
-  int src = lane;
-  warp_sort(key, src, lane);
-  Lane L;
-  L.live = key != INT_MAX;
-  L.p = E.p_off + (L.live ? wfirst + src : 0);
-  const unsigned same = __match_any_sync(kFull, key);
-  L.seg_end = 31 - __clz(same);
-  L.head = L.live && lane == __ffs(same) - 1;
-  L.lone = __all_sync(kFull, __popc(same) == 1);
-  return L;
-}
+  if (!live) st.base[0] = st.base[1] = st.base[2] = 0;
+  float *red = warp_red_buffer();
+  const Ranked R = rank_lanes(key, lane, red);
 
-// =================================================================== P2G
-// integrator.cu:84-100 (compute_svd) fused with :312-394 (p2g).
-__global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, const float *__restrict__ S,
-                                             float *__restrict__ Snext, float *__restrict__ tape) {
-  const int tile = blockIdx.x;
-  const DexEnv E = B.envs[B.tiles[2 * tile]];
-  const int first = B.tiles[2 * tile + 1];
-  const int N = B.n_particles;
-  const int lane = threadIdx.x & 31;
-  const Lane L = sorted_lane(B, E, S, first);
-  const int p = L.p;
-
-  const f3 x = ldf3(S, N, PX, p);
-  const f3 v = ldf3(S, N, PV, p);
-  const m33 F = ldm33(S, N, PF, p);
-  const m33 C = ldm33(S, N, PC, p);
-  const float m = L.live ? __ldg(B.mass + p) : 0.f;
+  const float m = live ? __ldg(B.mass + p) : 0.f;
   const float vol = __ldg(B.vol + p);
   const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
               ys = __ldg(B.mu_lam_yield + 2 * N + p);
-
   const m33 Et = deviation_tmp(F, C, E.dt);
   const SVD3 sv = svd3_from_deviation(Et);
   m33 Ft = Et;
   Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
   const Plastic pl = constitutive(sv, Ft, mu, lam, ys);
-  if (Snext != nullptr && L.live) stm33(Snext, N, PF, p, pl.newF);
-  if (tape != nullptr && L.live) store_tape(tape, N, p, sv, pl.P);
+  if (Fout != nullptr && live) stm33(Fout, N, PF, p, pl.newF);
+  if (tape != nullptr && live) store_tape(tape, N, p, sv, pl.P);
 
-  const float scale = L.live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
+  const float scale = live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
   const m33 A = pl.P * scale + C * m;
   const f3 mom = v * m;
-
-  Stencil st;
-  make_stencil(x, E.inv_dx, st);
   float *grid = slot_grid(B, X);
 
-#if DEX_SCATTER
-  const unsigned heads = __ballot_sync(kFull, L.head);
-  const int n_live = __popc(__ballot_sync(kFull, L.live));
-  if (__popc(heads) > kDirectSegs) {
+  if (__popc(R.heads) > kDirectSegs) {
     // nearly one particle per cell: per-lane vector atomics
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -358,13 +355,12 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
           const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
                               ((float)k - st.fx[2]) * E.dx);
           const f3 c = (mom + mv(A, dpos)) * w;
-          if (L.live) {
+          if (live) {
             const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
             red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, m * w);
           }
         }
   } else {
-    float *red = warp_red_buffer();
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
 #pragma unroll
@@ -376,40 +372,16 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
           const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
                               ((float)k - st.fx[2]) * E.dx);
           const f3 cv = (mom + mv(A, dpos)) * w;
-          red_put(red, c, lane, cv.x, cv.y, cv.z, m * w);
+          red_put(red, c, R.r, cv.x, cv.y, cv.z, m * w);
         }
       }
       __syncwarp();
-      red_walk(red, heads, n_live, 16 * g, g == 0 ? 16 : 11, st.base, E, grid, lane);
+      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, st.base, E, grid, lane);
       __syncwarp();
     }
   }
-#else
-#pragma unroll kNodeUnroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
-                            ((float)k - st.fx[2]) * E.dx);
-        f3 c = (mom + mv(A, dpos)) * w;
-        float cm = m * w;
-        if (!L.lone) {
-          c.x = seg_sum(c.x, lane, L.seg_end);
-          c.y = seg_sum(c.y, lane, L.seg_end);
-          c.z = seg_sum(c.z, lane, L.seg_end);
-          cm = seg_sum(cm, lane, L.seg_end);
-        }
-        if (L.head) {
-          int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
-          red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, cm);
-        }
-      }
-#endif
 
-  if (L.head) {
+  if (live && R.head) {
     const int nby = E.gy >> 2, nbz = E.gz >> 2;
     const int b0x = st.base[0] >> 2, b1x = (st.base[0] + 2) >> 2;
     const int b0y = st.base[1] >> 2, b1y = (st.base[1] + 2) >> 2;
@@ -418,6 +390,72 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
       for (int by = b0y; by <= b1y; ++by)
         for (int bz = b0z; bz <= b1z; ++bz) mark_block(B, X, E.blk_off + (bx * nby + by) * nbz + bz);
   }
+}
+
+// P2G of state S into slot X (projected F to Snext, nullable; tape nullable).
+__global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, const float *__restrict__ S,
+                                                           float *__restrict__ Snext, float *__restrict__ tape) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const int loc = first + threadIdx.x;
+  const bool in = loc < E.n;
+  const int p = E.p_off + (in ? loc : 0);
+  p2g_lane(B, E, X, p, in, ldf3(S, N, PX, p), ldf3(S, N, PV, p), ldm33(S, N, PF, p), ldm33(S, N, PC, p), Snext, tape,
+           lane);
+}
+
+// G2P of substep t fused with P2G of substep t + 1 (integrator.cu:1059-1109
+// then :84-100, :312-394).  From x_t in S and the velocities of grid slot Xg:
+// x, v, C of state t + 1 to Snext; then, with F_{t+1} from Snext's F planes,
+// the P2G of state t + 1 into slot Xs, its projected F to S2's F planes and
+// its tape.  S2 may be S: only x is read from S and only F is written to S2.
+__global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int Xg, int Xs, const float *S,
+                                                             float *Snext, float *S2, float *__restrict__ tape) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const int loc = first + threadIdx.x;
+  const bool in = loc < E.n;
+  const int p = E.p_off + (in ? loc : 0);
+  const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by their P2G
+  if (!ok) st.base[0] = st.base[1] = st.base[2] = 0;
+  const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, Xg));
+  f3 nv = mk3(0.f, 0.f, 0.f);
+  m33 nC = mzero();
+  const float c4 = 4.f * E.inv_dx;
+#pragma unroll kG2p2gUnroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
+        const float4 g = ok ? __ldg(vout + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+        const f3 gv = mk3(g.x, g.y, g.z);
+        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
+        nv += gv * w;
+        nC += outer(gv, dpos) * (w * c4);
+      }
+  f3 nx = x + nv * E.dt;
+  const float lo = E.ground_height * E.dx;
+  nx.x = fmaxf(fminf(nx.x, (E.gx - 3.f) * E.dx), lo);
+  nx.y = fmaxf(fminf(nx.y, (E.gy - 3.f) * E.dx), lo);
+  nx.z = fmaxf(fminf(nx.z, (E.gz - 3.f) * E.dx), lo);
+  if (ok) {
+    stf3(Snext, N, PX, p, nx);
+    stf3(Snext, N, PV, p, nv);
+    stm33(Snext, N, PC, p, nC);
+  }
+  p2g_lane(B, E, Xs, p, ok, nx, nv, ldm33(Snext, N, PF, p), nC, S2, tape, lane);
 }
 
 // ============================================================ grid update
@@ -537,21 +575,32 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   const int first = B.tiles[2 * tile + 1];
   const int N = B.n_particles;
   const int lane = threadIdx.x & 31;
-  const Lane L = sorted_lane(B, E, S, first);
-  const int p = L.p;
+  const int loc = first + threadIdx.x;
+  const int p = E.p_off + (loc < E.n ? loc : 0);
   const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  int key = INT_MAX;
+  if (loc < E.n) {
+    if (stencil_in_grid(E, st))
+      key = (st.base[0] * E.gy + st.base[1]) * E.gz + st.base[2];
+    else
+      atomicOr(B.error, DEXMPM_ERR_OUT_OF_GRID);
+  }
+  const bool live = key != INT_MAX;
+  if (!live) st.base[0] = st.base[1] = st.base[2] = 0;
+  float *red = warp_red_buffer();
+  const Ranked R = rank_lanes(key, lane, red);
   f3 gx = ldf3(Gnext, N, PX, p);
   f3 gnv = ldf3(Gnext, N, PV, p);
-  const m33 gC = L.live ? ldm33(Gnext, N, PC, p) : mzero();
+  const m33 gC = live ? ldm33(Gnext, N, PC, p) : mzero();
   const f3 nx = x + ldf3(Snext, N, PV, p) * E.dt;
   const float lo = E.ground_height * E.dx;
   if (nx.x > (E.gx - 3.f) * E.dx || nx.x < lo) gx.x = 0.f;
   if (nx.y > (E.gy - 3.f) * E.dx || nx.y < lo) gx.y = 0.f;
   if (nx.z > (E.gz - 3.f) * E.dx || nx.z < lo) gx.z = 0.f;
   gnv += gx * E.dt;
-  if (!L.live) gnv = mk3(0.f, 0.f, 0.f);
-  Stencil st;
-  make_stencil(x, E.inv_dx, st);
+  if (!live) gnv = mk3(0.f, 0.f, 0.f);
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
@@ -566,7 +615,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   auto node = [&](int i, int j, int k, int ci) -> f3 {
     const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
     const f3 gCd = step3(step3(step3(q0, g0c, i), g1c, j), g2c, k);
-    const float4 g4 = L.live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 g4 = live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
     const f3 gv = mk3(g4.x, g4.y, g4.z);
     wgv += gv * w;
     const float gw = dot(gnv, gv) + c4 * dot(gv, gCd);
@@ -575,11 +624,8 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
     gx += dw * gw;
     return gnv * w + gCd * (w * c4);
   };
-#if DEX_SCATTER
-  const unsigned heads = __ballot_sync(kFull, L.head);
-  const int n_live = __popc(__ballot_sync(kFull, L.live));
-  if (__popc(heads) > kDirectSegs) {
-#pragma unroll kNodeUnroll
+  if (__popc(R.heads) > kDirectSegs) {
+#pragma unroll kG2pGradUnroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
@@ -587,10 +633,9 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
         for (int k = 0; k < 3; ++k) {
           const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
           const f3 ggv = node(i, j, k, ci);
-          if (L.live) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
+          if (live) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
         }
   } else {
-    float *red = warp_red_buffer();
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
 #pragma unroll
@@ -600,34 +645,17 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
           const int i = n / 9, j = (n / 3) % 3, k = n % 3;
           const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
           const f3 ggv = node(i, j, k, ci);
-          red_put(red, c, lane, ggv.x, ggv.y, ggv.z, 0.f);
+          red_put(red, c, R.r, ggv.x, ggv.y, ggv.z, 0.f);
         }
       }
       __syncwarp();
-      red_walk(red, heads, n_live, 16 * g, g == 0 ? 16 : 11, st.base, E, vg, lane);
+      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, st.base, E, vg, lane);
       __syncwarp();
     }
   }
-#else
-#pragma unroll kNodeUnroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
-        f3 ggv = node(i, j, k, ci);
-        if (!L.lone) {
-          ggv.x = seg_sum(ggv.x, lane, L.seg_end);
-          ggv.y = seg_sum(ggv.y, lane, L.seg_end);
-          ggv.z = seg_sum(ggv.z, lane, L.seg_end);
-        }
-        if (L.head) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
-      }
-#endif
   // the C-gradient term of every node: sum_n gC^T v_n (-inv_dx c4 w_n)
   gx += mtv(gC, wgv) * (-E.inv_dx * c4);
-  if (L.live) stf3(G, N, PX, p, gx);
+  if (live) stf3(G, N, PX, p, gx);
 }
 
 // ===================================================== grid update adjoint
@@ -945,7 +973,7 @@ int grid_ctas(const DexBatch *b, const void *kernel, int id) {
 }
 
 // Dynamic shared memory of the scatter kernels for CTAs of `threads`.
-size_t scatter_smem(int threads) { return DEX_SCATTER ? (size_t)(threads / 32) * kScatterSmemPerWarp : 0; }
+size_t scatter_smem(int threads) { return (size_t)(threads / 32) * kScatterSmemPerWarp; }
 
 // Opt the scatter kernels in to the dynamic shared memory of 256-thread CTAs
 // (above the 48 KB default), once per device.
@@ -956,6 +984,7 @@ int scatter_attr_ready() {
   if (ready[dev].load(std::memory_order_acquire)) return DEXMPM_OK;
   const int bytes = (int)scatter_smem(256);
   if (cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
+      cudaFuncSetAttribute(k_g2p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
       cudaFuncSetAttribute(k_g2p_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
     return DEXMPM_ERR_LAUNCH;
   ready[dev].store(1, std::memory_order_release);
@@ -1006,6 +1035,18 @@ int dexmpm_g2p(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm
   if (!valid(b) || !S || !Snext || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   k_g2p<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext);
+  return check_launch();
+}
+
+int dexmpm_g2p2g(const DexBatch *b, int slot_g, int slot_s, const float *S, float *Snext, float *S2, float *tape,
+                 dexmpm_stream_t stream) {
+  if (!valid(b) || !S || !Snext || !S2 || Snext == S || Snext == S2 || !slot_ok(b, slot_g) || !slot_ok(b, slot_s) ||
+      slot_g == slot_s)
+    return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  if (int rc = scatter_attr_ready()) return rc;
+  k_g2p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot_g, slot_s, S, Snext,
+                                                                                        S2, tape);
   return check_launch();
 }
 

@@ -252,6 +252,43 @@ class BatchEngine:
         self.launches += 3
         return slot
 
+    def run_substeps(self, sts: Sequence[torch.Tensor], poses: torch.Tensor, kept: bool = False,
+                     tapes: Optional[torch.Tensor] = None):
+        """T = len(sts) - 1 forward substeps from sts[0] to sts[T] (sts[t], 0 < t
+        < T, hold the intermediate states; sts[t] and sts[t + 2] may be one
+        buffer), with body poses poses[0..T].  The G2P of every substep but
+        the last is fused with the next substep's P2G.  Slots: the forward
+        pair (kept=False) or slot 2 + t kept for the adjoint of substep t
+        (kept=True), with tapes[t] written when given."""
+        T = len(sts) - 1
+        if T < 1:
+            return
+        L, bp, sp = self.lib, self._bp, N.stream_ptr()
+
+        def take(t):
+            if kept:
+                assert 2 + t < self.n_grid_slots
+                return 2 + t, -1
+            slot = self.fslot
+            self.fslot ^= 1
+            return slot, slot ^ 1
+
+        def tape(t):
+            return N.ptr(tapes[t]) if tapes is not None else None
+
+        slot, clear = take(0)
+        N.check(L.dexmpm_p2g(bp, slot, N.ptr(sts[0]), N.ptr(sts[1]), tape(0), sp), "dexmpm_p2g")
+        N.check(L.dexmpm_grid_op(bp, slot, clear, N.ptr(poses[0]), N.ptr(poses[1]), sp), "dexmpm_grid_op")
+        for t in range(T - 1):
+            nslot, clear = take(t + 1)
+            N.check(L.dexmpm_g2p2g(bp, slot, nslot, N.ptr(sts[t]), N.ptr(sts[t + 1]), N.ptr(sts[t + 2]), tape(t + 1),
+                                   sp), "dexmpm_g2p2g")
+            N.check(L.dexmpm_grid_op(bp, nslot, clear, N.ptr(poses[t + 1]), N.ptr(poses[t + 2]), sp),
+                    "dexmpm_grid_op")
+            slot = nslot
+        N.check(L.dexmpm_g2p(bp, slot, N.ptr(sts[T - 1]), N.ptr(sts[T]), sp), "dexmpm_g2p")
+        self.launches += 2 * T + 1
+
     def substep_grad(self, s, s_next, g_next, g, pose, next_pose, bgrad, next_bgrad, slot: Optional[int] = None,
                      tape: Optional[torch.Tensor] = None):
         """Adjoint of one substep: G2P, grid and P2G adjoints.  With `slot` the
@@ -343,25 +380,18 @@ class Rollout:
         return self.ckpt[k] if self.E.grad else self.ckpt[k % 2]
 
     def _forward_step(self, k: int):
-        """Env step k: ckpt[k] -> ckpt[k+1] through T substeps."""
-        T, E = self.T, self.E
-        src = self._ckpt(k)
-        for s in range(T):
-            t = k * T + s
-            dst = self._ckpt(k + 1) if s == T - 1 else self.ring[s % 2]
-            E.substep(src, dst, self.poses[t], self.poses[t + 1])
-            src = dst
+        """Env step k: ckpt[k] -> ckpt[k+1] through T substeps (two ring
+        buffers for the intermediate states)."""
+        T = self.T
+        sts = [self._ckpt(k)] + [self.ring[t % 2] for t in range(1, T)] + [self._ckpt(k + 1)]
+        self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1])
 
     def _forward_step_kept(self, k: int):
         """Env step k as the backward recomputes it: states into the ring,
         grids kept in slots 2..T+1, the tape written; result in ckpt[k+1]."""
-        T, E = self.T, self.E
-        src = self.ckpt[k]
-        for s in range(T):
-            t = k * T + s
-            dst = self.ckpt[k + 1] if s == T - 1 else self.ring[s + 1]
-            E.substep(src, dst, self.poses[t], self.poses[t + 1], slot=2 + s, tape=self._tape(s))
-            src = dst
+        T = self.T
+        sts = [self.ckpt[k]] + [self.ring[t] for t in range(1, T)] + [self.ckpt[k + 1]]
+        self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=self.tape)
 
     def forward_step(self, k: int):
         self._run(self._fwd_graphs, k, self._forward_step)
@@ -393,12 +423,14 @@ class Rollout:
         kept them, then run the adjoint substeps in reverse.  Result in
         gbuf[1]."""
         T, E = self.T, self.E
-        if recompute:
+        if recompute and self.keep_grids:
+            sts = [self.ckpt[k]] + [self.ring[t] for t in range(1, T + 1)]
+            E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=self.tape)
+        elif recompute:
             src = self.ckpt[k]
             for s in range(T):
                 t = k * T + s
-                E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1],
-                          slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
+                E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1])
                 src = self.ring[s + 1]
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):

@@ -95,13 +95,11 @@ class _Batch:
         self.graphs = {}
 
     def _forward(self):
-        for s in range(self.T):
-            self.E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1])
+        self.E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses)
 
     def _backward(self):
         E = self.E
-        for s in range(self.T):
-            E.substep(self.slot[s], self.slot[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s, tape=self.tape[s])
+        E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.slot[s], self.slot[s + 1], g_next, g, self.poses[s], self.poses[s + 1],

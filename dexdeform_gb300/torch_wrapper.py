@@ -53,14 +53,11 @@ class DiffSim:
 
     # eager bodies of the two graphs
     def _fwd(self):
-        E = self.E
-        for s in range(self.T):
-            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1])
+        self.E.run_substeps([self.ring[s] for s in range(self.T + 1)], self.poses)
 
     def _bwd(self):
         E = self.E
-        for s in range(self.T):
-            E.substep(self.ring[s], self.ring[s + 1], self.poses[s], self.poses[s + 1], slot=2 + s, tape=self.tape[s])
+        E.run_substeps([self.ring[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(self.T - 1, -1, -1):
             E.substep_grad(self.ring[s], self.ring[s + 1], g_next, g, self.poses[s], self.poses[s + 1],

@@ -230,6 +230,16 @@ int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pos
 /* G2P from grid slot `slot`: x, v, C of next_s from s. */
 int dexmpm_g2p(const DexBatch *b, int slot, const float *s, float *next_s, dexmpm_stream_t stream);
 
+/* G2P of substep t from grid slot slot_g fused with the P2G of substep t + 1
+ * into slot slot_s: x, v, C of state t + 1 to next_s from x of state s; then,
+ * with the F of state t + 1 already in next_s (written by the P2G of substep
+ * t), that state's SVD, stress and scatter, its projected F to s2's F planes
+ * and its tape (nullable).  s2 may be s (only x is read from s, only F is
+ * written to s2).  Same results as dexmpm_g2p(slot_g) + dexmpm_p2g(slot_s)
+ * without reloading state t + 1 or a second launch. */
+int dexmpm_g2p2g(const DexBatch *b, int slot_g, int slot_s, const float *s, float *next_s, float *s2, float *tape,
+                 dexmpm_stream_t stream);
+
 /* One forward substep: dexmpm_p2g + dexmpm_grid_op + dexmpm_g2p. */
 int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *s, float *next_s, const float *pose,
                    const float *next_pose, float *tape, dexmpm_stream_t stream);

@@ -385,3 +385,35 @@ def test_kept_last_env_step_equals_recompute(cuda):
     for other in outs[1:]:
         for (a, b), tol in zip(zip(outs[0], other), (2e-4, 5e-4, 5e-4)):
             assert rel(a.cpu().numpy(), b.cpu().numpy()) < tol
+
+
+def test_fused_substeps_equal_unfused(cuda):
+    """run_substeps (each G2P fused with the next P2G) against the same T
+    substeps launched one kernel at a time (P2G, grid update, G2P), in the
+    forward slot protocol and with kept slots and a tape."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec
+    envs = W.batch_envs(6, n_envs=3, steps=10, n_lo=500, n_hi=3000)
+    T = 10
+    finals = []
+    for mode in ("unfused", "fused", "fused_kept"):
+        E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=T + 2)
+        poses = torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
+                             device="cuda")
+        sts = E.new_slots(T + 1)
+        sts[0].copy_(E.pack_state([W.perturb_state(e, seed=2, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+                                   for e in envs]))
+        if mode == "unfused":
+            for t in range(T):
+                E.substep(sts[t], sts[t + 1], poses[t], poses[t + 1])
+        elif mode == "fused":
+            E.run_substeps([sts[t] for t in range(T + 1)], poses)
+        else:
+            tapes = E.new_tape(T)
+            E.run_substeps([sts[t] for t in range(T + 1)], poses, kept=True, tapes=tapes)
+            E.clear_slots(2, 2 + T)
+        assert E.error_word() == 0
+        finals.append(sts[T].clone())
+    # float-atomic ordering only: ~1e-5 after 10 substeps from this state
+    for other in finals[1:]:
+        assert rel(other.cpu().numpy(), finals[0].cpu().numpy()) < 1e-4
