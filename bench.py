@@ -421,8 +421,8 @@ ALG_BYTES = {
 
 # DRAM bytes (read + write) per particle of one launch, from ncu captures
 # on the 64-env batch (profiles/k_*_batch64.md)
-NCU_DRAM_BYTES_PER_PARTICLE = {"p2g": 84.951296e6 / 654552, "p2g_grad": 239.917568e6 / 654552,
-                               "g2p_grad": 63.15264e6 / 654552}
+NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 239.917568e6 / 654552, "g2p2g_tape": 143.249408e6 / 654552,
+                               "g2p2g": 64.70016e6 / 654552}
 
 # launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
@@ -449,7 +449,7 @@ def roofline(E, kt, cells):
             "traffic": int(NCU_DRAM_BYTES_PER_PARTICLE[top] * n) if top in NCU_DRAM_BYTES_PER_PARTICLE else None,
             "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the kernel on the "
                             "same 64-env batch (654,552 particles, 5 substeps per env step), per particle x n; "
-                            "profiles/<kernel>_batch64.md"}
+                            "profiles/k_<kernel>_batch64.md"}
 
 
 def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
