@@ -340,7 +340,11 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
 
   const float scale = live ? -E.dt * vol * 4.f * E.inv_dx * E.inv_dx : 0.f;
   const m33 A = pl.P * scale + C * m;
-  const f3 mom = v * m;
+  // node momentum mom + A dpos, dpos = ((i, j, k) - fx) dx, as b0 + i a0 +
+  // j a1 + k a2 with the columns a of A dx: the node offsets are constants of
+  // the unrolled loops, so the sums are shared between nodes
+  const f3 a0 = mcol(A, 0) * E.dx, a1 = mcol(A, 1) * E.dx, a2 = mcol(A, 2) * E.dx;
+  const f3 b0 = v * m - (a0 * st.fx[0] + a1 * st.fx[1] + a2 * st.fx[2]);
   float *grid = slot_grid(B, X);
 
   if (__popc(R.heads) > kDirectSegs) {
@@ -352,9 +356,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-          const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
-                              ((float)k - st.fx[2]) * E.dx);
-          const f3 c = (mom + mv(A, dpos)) * w;
+          const f3 c = step3(step3(step3(b0, a0, i), a1, j), a2, k) * w;
           if (live) {
             const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
             red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, m * w);
@@ -369,9 +371,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
         if (n < 27) {
           const int i = n / 9, j = (n / 3) % 3, k = n % 3;
           const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-          const f3 dpos = mk3(((float)i - st.fx[0]) * E.dx, ((float)j - st.fx[1]) * E.dx,
-                              ((float)k - st.fx[2]) * E.dx);
-          const f3 cv = (mom + mv(A, dpos)) * w;
+          const f3 cv = step3(step3(step3(b0, a0, i), a1, j), a2, k) * w;
           red_put(red, c, R.r, cv.x, cv.y, cv.z, m * w);
         }
       }
@@ -428,9 +428,10 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
   const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by their P2G
   if (!ok) st.base[0] = st.base[1] = st.base[2] = 0;
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, Xg));
-  f3 nv = mk3(0.f, 0.f, 0.f);
-  m33 nC = mzero();
-  const float c4 = 4.f * E.inv_dx;
+  // v = sum w v_n;  C = 4 inv_dx sum w v_n ((i, j, k) - fx)^T
+  //   = 4 inv_dx (sum w v_n (i, j, k)^T - v fx^T), the node offsets being
+  //   constants of the unrolled loops
+  f3 nv = mk3(0.f, 0.f, 0.f), ci = mk3(0.f, 0.f, 0.f), cj = mk3(0.f, 0.f, 0.f), ck = mk3(0.f, 0.f, 0.f);
 #pragma unroll kG2p2gUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -440,11 +441,21 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
         const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
         const float4 g = ok ? __ldg(vout + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
-        const f3 gv = mk3(g.x, g.y, g.z);
-        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
-        nv += gv * w;
-        nC += outer(gv, dpos) * (w * c4);
+        const f3 a = mk3(g.x, g.y, g.z) * w;
+        nv += a;
+        if (i) ci += i == 1 ? a : a * 2.f;
+        if (j) cj += j == 1 ? a : a * 2.f;
+        if (k) ck += k == 1 ? a : a * 2.f;
       }
+  const float c4 = 4.f * E.inv_dx;
+  m33 nC;
+  const f3 col[3] = {ci - nv * st.fx[0], cj - nv * st.fx[1], ck - nv * st.fx[2]};
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    nC.a[r][0] = (r == 0 ? col[0].x : r == 1 ? col[0].y : col[0].z) * c4;
+    nC.a[r][1] = (r == 0 ? col[1].x : r == 1 ? col[1].y : col[1].z) * c4;
+    nC.a[r][2] = (r == 0 ? col[2].x : r == 1 ? col[2].y : col[2].z) * c4;
+  }
   f3 nx = x + nv * E.dt;
   const float lo = E.ground_height * E.dx;
   nx.x = fmaxf(fminf(nx.x, (E.gx - 3.f) * E.dx), lo);
