@@ -46,6 +46,9 @@ using namespace dexmpm;
 #ifndef DEX_G2P2G_MINB
 #define DEX_G2P2G_MINB 3
 #endif
+#ifndef DEX_P2G_GRAD_UNROLL
+#define DEX_P2G_GRAD_UNROLL 3
+#endif
 #ifndef DEX_G2P_GRAD_UNROLL
 #define DEX_G2P_GRAD_UNROLL 3
 #endif
@@ -66,6 +69,7 @@ using namespace dexmpm;
 constexpr int kNodeUnroll = DEX_NODE_UNROLL;
 constexpr int kG2p2gUnroll = DEX_G2P2G_UNROLL;
 constexpr int kG2pGradUnroll = DEX_G2P_GRAD_UNROLL;
+constexpr int kP2gGradUnroll = DEX_P2G_GRAD_UNROLL;
 
 namespace {
 
@@ -836,15 +840,11 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   // A dpos = a0 + i A0 dx + j A1 dx + k A2 dx.
   const f3 a0c = mcol(A, 0) * E.dx, a1c = mcol(A, 1) * E.dx, a2c = mcol(A, 2) * E.dx;
   const f3 a0 = -(a0c * st.fx[0] + a1c * st.fx[1] + a2c * st.fx[2]);
-  float dp[3][3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) dp[d][i] = ((float)i - st.fx[d]) * E.dx;
   const f3 u = v * m;
-  m33 Gs = mzero();
+  // Gs = sum N gov ((i, j, k) - fx)^T dx = (sum N gov (i, j, k)^T - gw fx^T) dx
   f3 g_x = mk3(0.f, 0.f, 0.f), gw = mk3(0.f, 0.f, 0.f);
-#pragma unroll kNodeUnroll
+  f3 si = mk3(0.f, 0.f, 0.f), sj = mk3(0.f, 0.f, 0.f), sk = mk3(0.f, 0.f, 0.f);
+#pragma unroll kP2gGradUnroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -857,11 +857,20 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
                           st.w[0][i] * st.w[1][j] * w1[2][k]);
         const f3 Ad = step3(step3(step3(a0, a0c, i), a1c, j), a2c, k);
         const f3 a = gov * Nw;
-        Gs += outer(a, mk3(dp[0][i], dp[1][j], dp[2][k]));
         gw += a;
+        if (i) si += i == 1 ? a : a * 2.f;
+        if (j) sj += j == 1 ? a : a * 2.f;
+        if (k) sk += k == 1 ? a : a * 2.f;
         g_x += gN * (g4.w * m + dot(u, gov) + dot(Ad, gov));
       }
   g_x -= mtv(A, gw);
+  m33 Gs;
+  {
+    const f3 c0 = (si - gw * st.fx[0]) * E.dx, c1 = (sj - gw * st.fx[1]) * E.dx, c2 = (sk - gw * st.fx[2]) * E.dx;
+    Gs.a[0][0] = c0.x; Gs.a[1][0] = c0.y; Gs.a[2][0] = c0.z;
+    Gs.a[0][1] = c1.x; Gs.a[1][1] = c1.y; Gs.a[2][1] = c1.z;
+    Gs.a[0][2] = c2.x; Gs.a[1][2] = c2.y; Gs.a[2][2] = c2.z;
+  }
   const m33 g_stress = Gs * gss, g_C = Gs * m;
   const f3 g_v = gw * m;
   if constexpr (kTape) forward_state();
