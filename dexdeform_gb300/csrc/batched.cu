@@ -173,11 +173,6 @@ __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, 
   atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
-  return v;
-}
 
 // ------------------------------------------------ transposed warp scatter
 // The scatter kernels add 27 node contributions per particle to the grid.
@@ -262,6 +257,40 @@ __device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int 
       atomicAdd(reinterpret_cast<float2 *>(grid + 4 * (size_t)ci + 2 * h), acc);
     }
   }
+}
+
+// Reduce-scatter of 16 values over the warp: on return lane l holds the
+// warp sum of value ((l >> 4) & 1) * 8 + ((l >> 3) & 1) * 4 + ((l >> 2) & 1) * 2
+// + ((l >> 1) & 1) (lanes l and l ^ 1 hold the same value).  16 shuffles in
+// place of 16 x 5 for separate butterflies.
+__device__ __forceinline__ float warp_reduce_scatter16(float v[16], int lane) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const bool up = lane & 16;
+    const float r = __shfl_xor_sync(kFull, up ? v[i] : v[i + 8], 16);
+    v[i] = (up ? v[i + 8] : v[i]) + r;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool up = lane & 8;
+    const float r = __shfl_xor_sync(kFull, up ? v[i] : v[i + 4], 8);
+    v[i] = (up ? v[i + 4] : v[i]) + r;
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool up = lane & 4;
+    const float r = __shfl_xor_sync(kFull, up ? v[i] : v[i + 2], 4);
+    v[i] = (up ? v[i + 2] : v[i]) + r;
+  }
+  {
+    const bool up = lane & 2;
+    const float r = __shfl_xor_sync(kFull, up ? v[0] : v[1], 2);
+    v[0] = (up ? v[1] : v[0]) + r;
+  }
+  return v[0] + __shfl_xor_sync(kFull, v[0], 1);
+}
+__device__ __forceinline__ int reduce_scatter16_index(int lane) {
+  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
 }
 
 __device__ __forceinline__ void mark_block(const DexBatch &B, int X, int blk) {
@@ -621,23 +650,24 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   float *vg = B.vout_grad;
   const float c4 = 4.f * E.inv_dx;
-  // gC dpos (dpos in cells) = q0 + i gC0 + j gC1 + k gC2
-  const f3 g0c = mcol(gC, 0), g1c = mcol(gC, 1), g2c = mcol(gC, 2);
-  const f3 q0 = -(g0c * st.fx[0] + g1c * st.fx[1] + g2c * st.fx[2]);
+  // per node: t = gnv + c4 gC dpos (dpos in cells) = t0 + i t1 + j t2 + k t3,
+  // the node's dL/dv_out is w t and its weight-gradient factor v_out . t
+  const f3 t1 = mcol(gC, 0) * c4, t2 = mcol(gC, 1) * c4, t3 = mcol(gC, 2) * c4;
+  const f3 t0 = gnv - (t1 * st.fx[0] + t2 * st.fx[1] + t3 * st.fx[2]);
   f3 wgv = mk3(0.f, 0.f, 0.f);  // sum of w v_out over the nodes
   // one stencil node: gather-side gradient terms into gx; returns the node's
   // dL/dv_out contribution
   auto node = [&](int i, int j, int k, int ci) -> f3 {
     const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-    const f3 gCd = step3(step3(step3(q0, g0c, i), g1c, j), g2c, k);
+    const f3 t = step3(step3(step3(t0, t1, i), t2, j), t3, k);
     const float4 g4 = live ? __ldg(vout + ci) : make_float4(0.f, 0.f, 0.f, 0.f);
     const f3 gv = mk3(g4.x, g4.y, g4.z);
     wgv += gv * w;
-    const float gw = dot(gnv, gv) + c4 * dot(gv, gCd);
+    const float gw = dot(gv, t);
     const f3 dw = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
                       st.w[0][i] * st.w[1][j] * w1[2][k]);
     gx += dw * gw;
-    return gnv * w + gCd * (w * c4);
+    return t * w;
   };
   if (__popc(R.heads) > kDirectSegs) {
 #pragma unroll kG2pGradUnroll
@@ -681,7 +711,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
 // dL/d(mv, m) written (zero where there is no mass), and dL/dv_out and the
 // slot's grid are zeroed after they are read, so the next use finds them
 // clean; the last CTA resets the slot's list.
-__global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
+__global__ void __launch_bounds__(256, 3) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
                                                       const float *__restrict__ next_pose, float *__restrict__ bgrad,
                                                       float *__restrict__ next_bgrad) {
   const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
@@ -750,15 +780,21 @@ __global__ void __launch_bounds__(256) k_grid_op_grad(DexBatch B, int X, const f
         load_shape(B.body_shape, E.body_off + b, sh);
         contact_backward(gx, vin[b], gv, cur, nxt, sh, E.dt, gc, gn, exact_capsule);
       }
+      // the 14 pose-gradient values (7 at each end of the substep) summed
+      // over the warp, then added by 14 lanes in one atomic instruction
+      float vals[16];
 #pragma unroll
       for (int c = 0; c < 7; ++c) {
-        float a = warp_sum(gc[c]);
-        float n = warp_sum(gn[c]);
-        if (lane == 0) {
-          const int o = 8 * (E.body_off + b) + (c < 3 ? c : c + 1);
-          atomicAdd(bgrad + o, a);
-          atomicAdd(next_bgrad + o, n);
-        }
+        vals[c] = gc[c];
+        vals[7 + c] = gn[c];
+      }
+      vals[14] = vals[15] = 0.f;
+      const float total = warp_reduce_scatter16(vals, lane);
+      const int vi = reduce_scatter16_index(lane);
+      if ((lane & 1) == 0 && vi < 14) {
+        const int c = vi < 7 ? vi : vi - 7;
+        const int o = 8 * (E.body_off + b) + (c < 3 ? c : c + 1);
+        atomicAdd((vi < 7 ? bgrad : next_bgrad) + o, total);
       }
     }
     if (in_list) {
