@@ -7,11 +7,11 @@
 //   * grid phases (grid update and its adjoint): a persistent grid of at most
 //     the resident number of CTAs walking the active-block list, 64 threads
 //     per block.
-// Scatters (P2G and the G2P adjoint) pre-reduce in the warp: the warp orders
-// its lanes by stencil base cell (bitonic sort on shuffles), equal bases form
-// segments, and each segment's 27 node sums are formed through a transposed
-// shared-memory buffer and added with one 8-byte vector atomic per node and
-// component pair.  Grid storage is an array of slots (mass/momentum grid,
+// Scatters (P2G and the G2P adjoint) pre-reduce in the warp: the warp groups
+// its lanes by stencil base cell (one match instruction and a prefix sum of
+// the group sizes), equal bases form segments, and each segment's 27 node
+// sums are formed through a transposed shared-memory buffer and added with
+// one 8-byte vector atomic per node and component pair.  Grid storage is an array of slots (mass/momentum grid,
 // post-update velocities, active-block list per slot): forward substeps
 // alternate two slots and each grid update clears the slot the previous
 // substep used; the adjoint of an env step reads the slots its recomputed
@@ -144,30 +144,29 @@ __device__ __forceinline__ int cell_index(const DexEnv &E, int x, int y, int z) 
   return (blk << 6) + ((x & 3) << 4) + ((y & 3) << 2) + (z & 3);
 }
 
+// Cell indices of the 27 stencil nodes as sums of per-axis terms:
+// cell_index(E, b0 + i, b1 + j, b2 + k) = x[i] + y[j] + z[k].
+struct NodeCells {
+  int x[3], y[3], z[3];
+  __device__ __forceinline__ int at(int i, int j, int k) const { return x[i] + y[j] + z[k]; }
+};
+__device__ __forceinline__ NodeCells node_cells(const DexEnv &E, const int base[3]) {
+  const int nbz = E.gz >> 2, nyz = (E.gy >> 2) * nbz;
+  NodeCells c;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int x = base[0] + d, y = base[1] + d, z = base[2] + d;
+    c.x[d] = ((E.blk_off + (x >> 2) * nyz) << 6) + ((x & 3) << 4);
+    c.y[d] = (((y >> 2) * nbz) << 6) + ((y & 3) << 2);
+    c.z[d] = ((z >> 2) << 6) + (z & 3);
+  }
+  return c;
+}
+
 __device__ __forceinline__ bool stencil_in_grid(const DexEnv &E, const Stencil &st) {
   return st.base[0] >= 0 && st.base[1] >= 0 && st.base[2] >= 0 && st.base[0] + 2 < E.gx &&
          st.base[1] + 2 < E.gy && st.base[2] + 2 < E.gz;
 }
-
-// 32-wide bitonic sort of (key, idx) across the warp, ascending by (key, idx).
-__device__ __forceinline__ void warp_sort(int &key, int &idx, int lane) {
-#pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      int ok = __shfl_xor_sync(kFull, key, j);
-      int oi = __shfl_xor_sync(kFull, idx, j);
-      bool up = (lane & k) == 0;
-      bool lower = (lane & j) == 0;
-      bool other_less = ok < key || (ok == key && oi < idx);
-      if ((lower == up) ? other_less : !other_less) {
-        key = ok;
-        idx = oi;
-      }
-    }
-  }
-}
-
 
 __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, float d) {
   atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
@@ -176,17 +175,17 @@ __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, 
 
 // ------------------------------------------------ transposed warp scatter
 // The scatter kernels add 27 node contributions per particle to the grid.
-// Every lane keeps its own particle; the warp orders its lanes by (stencil
-// base, lane) with a 32-wide bitonic sort on shuffles, so that equal bases
-// (the same 27 target cells) form contiguous segments of positions.  Per group
-// of up to 16 nodes every lane stores its float4 per node at its position's
-// column of a per-warp shared buffer; then lane l owns component pair (l & 1)
-// of node (l >> 1), sums it over each segment with plain loads, and the
-// segment's total goes to the grid in one 8-byte vector atomic.  Rows are
-// padded to 132 floats so that both the stores (16 B per lane) and the loads
-// (8 B per lane, one row per lane pair) are free of bank conflicts.  Warps
-// with more than DEX_DIRECT_SEGS segments (about one particle per cell) add
-// their contributions with per-lane float4 atomics instead.
+// Every lane keeps its own particle; the warp gives its lanes positions such
+// that equal stencil bases (the same 27 target cells) form contiguous segments
+// (lanes of equal key found with a match instruction, segments placed by a
+// warp prefix sum of their sizes).  Per group of up to 16 nodes every lane
+// stores its float4 per node at its position's column of a per-warp shared
+// buffer; then lane l owns component pair (l & 1) of node (l >> 1), sums it
+// over each segment with plain loads, and the segment's total goes to the
+// grid in one 8-byte vector atomic.  Rows are padded to 132 floats so that the
+// loads (8 B per lane, one row per lane pair) are free of bank conflicts.
+// Warps with more than DEX_DIRECT_SEGS segments (about one particle per cell)
+// add their contributions with per-lane float4 atomics instead.
 constexpr int kRedRow = 132;                      // floats per node row (32 lanes x 4 + 4 pad)
 constexpr int kRedWarpFloats = 16 * kRedRow + 32;  // 16 node rows + the position table
 constexpr int kDirectSegs = DEX_DIRECT_SEGS;
@@ -197,8 +196,8 @@ __device__ __forceinline__ float *warp_red_buffer() {
   return reinterpret_cast<float *>(s_dyn) + (threadIdx.x >> 5) * kRedWarpFloats;
 }
 
-// This lane's position in the warp's (key, lane) order and the segment
-// structure of that order (key INT_MAX: no contribution, sorts last).
+// This lane's position in the warp's segment order and the segment
+// structure of that order (key INT_MAX: no contribution, placed last).
 struct Ranked {
   int r;           // position of this lane
   int src;         // lane at position `lane` (for per-segment lookups)
@@ -207,18 +206,31 @@ struct Ranked {
   bool head;       // this lane starts its segment
 };
 __device__ __forceinline__ Ranked rank_lanes(int key, int lane, float *red) {
-  int k = key, src = lane;
-  warp_sort(k, src, lane);  // lane q now holds position q
-  int *pos = reinterpret_cast<int *>(red + 16 * kRedRow);
-  pos[src] = lane;
-  __syncwarp();
+  // Lanes with equal keys found in one match; segments are ordered by their
+  // lowest lane, positions within a segment by lane, dead lanes (INT_MAX)
+  // after all live ones.
+  const unsigned same = __match_any_sync(kFull, key);
+  const unsigned below = (1u << lane) - 1u;
+  const bool live = key != INT_MAX;
+  const bool lead = (same & below) == 0u;
+  const int size = (lead && live) ? __popc(same) : 0;
+  int incl = size;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int t = __shfl_up_sync(kFull, incl, d);
+    if (lane >= d) incl += t;
+  }
   Ranked R;
-  R.r = pos[lane];
-  R.src = src;
-  const int prev = __shfl_up_sync(kFull, k, 1);
-  R.heads = __ballot_sync(kFull, k != INT_MAX && (lane == 0 || prev != k));
-  R.n_live = __popc(__ballot_sync(kFull, k != INT_MAX));
-  R.head = (R.heads >> R.r) & 1u;
+  R.n_live = __shfl_sync(kFull, incl, 31);
+  const int seg0 = __shfl_sync(kFull, incl - size, __ffs(same) - 1);
+  const int within = __popc(same & below);
+  R.r = (live ? seg0 : R.n_live) + within;
+  R.head = lead && live;
+  R.heads = __reduce_or_sync(kFull, R.head ? (1u << seg0) : 0u);
+  int *pos = reinterpret_cast<int *>(red + 16 * kRedRow);
+  pos[R.r] = lane;
+  __syncwarp();
+  R.src = pos[lane];
   __syncwarp();
   return R;
 }
@@ -382,6 +394,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
 
   if (__popc(R.heads) > kDirectSegs) {
     // nearly one particle per cell: per-lane vector atomics
+    const NodeCells nc = node_cells(E, st.base);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -391,7 +404,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
           const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
           const f3 c = step3(step3(step3(b0, a0, i), a1, j), a2, k) * w;
           if (live) {
-            const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+            const int ci = nc.at(i, j, k);
             red_add4(grid + 4 * (size_t)ci, c.x, c.y, c.z, m * w);
           }
         }
@@ -460,6 +473,7 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
   make_stencil(x, E.inv_dx, st);
   const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by their P2G
   if (!ok) st.base[0] = st.base[1] = st.base[2] = 0;
+  const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, Xg));
   // v = sum w v_n;  C = 4 inv_dx sum w v_n ((i, j, k) - fx)^T
   //   = 4 inv_dx (sum w v_n (i, j, k)^T - v fx^T), the node offsets being
@@ -472,7 +486,7 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g = ok ? __ldg(vout + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k))
+        const float4 g = ok ? __ldg(vout + nc.at(i, j, k))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
         const f3 a = mk3(g.x, g.y, g.z) * w;
         nv += a;
@@ -582,6 +596,7 @@ __global__ void __launch_bounds__(256) k_g2p(DexBatch B, int X, const float *__r
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   if (!stencil_in_grid(E, st)) return;  // reported by P2G
+  const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   f3 nv = mk3(0.f, 0.f, 0.f);
   m33 nC = mzero();
@@ -593,7 +608,7 @@ __global__ void __launch_bounds__(256) k_g2p(DexBatch B, int X, const float *__r
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g = __ldg(vout + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k));
+        const float4 g = __ldg(vout + nc.at(i, j, k));
         const f3 gv = mk3(g.x, g.y, g.z);
         const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
         nv += gv * w;
@@ -647,6 +662,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   if (!live) gnv = mk3(0.f, 0.f, 0.f);
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
+  const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
   float *vg = B.vout_grad;
   const float c4 = 4.f * E.inv_dx;
@@ -676,7 +692,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
       for (int j = 0; j < 3; ++j)
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+          const int ci = nc.at(i, j, k);
           const f3 ggv = node(i, j, k, ci);
           if (live) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
         }
@@ -688,7 +704,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
         const int n = 16 * g + c;
         if (n < 27) {
           const int i = n / 9, j = (n / 3) % 3, k = n % 3;
-          const int ci = cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k);
+          const int ci = nc.at(i, j, k);
           const f3 ggv = node(i, j, k, ci);
           red_put(red, c, R.r, ggv.x, ggv.y, ggv.z, 0.f);
         }
@@ -818,6 +834,7 @@ __global__ void __launch_bounds__(256, 3) k_grid_op_grad(DexBatch B, int X, cons
 }
 
 // ============================================================ P2G adjoint
+
 // integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad).
 // Adds to the x gradient written by k_g2p_grad and writes v, F, C gradients.
 // With kTape the SVD of F_tmp comes from the tape the recomputed forward
@@ -869,6 +886,7 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
 
   float w1[3][3];
   make_dweights(st, E.inv_dx, w1);
+  const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ ig = reinterpret_cast<const float4 *>(B.in_grad);
   // per node n with weight N_n, offset dpos_n and incoming dL/d(mv), dL/dm
   // (gov_n, gm_n):  dL/dstress = gss Gs, dL/dC = m Gs with Gs = sum N gov dpos^T;
@@ -887,7 +905,7 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const float Nw = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g4 = __ldg(ig + cell_index(E, st.base[0] + i, st.base[1] + j, st.base[2] + k));
+        const float4 g4 = __ldg(ig + nc.at(i, j, k));
         const f3 gov = mk3(g4.x, g4.y, g4.z);
         const f3 gN = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
                           st.w[0][i] * st.w[1][j] * w1[2][k]);
