@@ -462,8 +462,8 @@ DX_HD Plastic constitutive(const SVD3 &sv, const m33 &Ftmp, float mu, float lam,
   if (dg > 0.f) {
     float k = dg / ehn;
     float ep[3] = {e[0] - k * eh.x, e[1] - k * eh.y, e[2] - k * eh.z};
-    f3 ee = mk3(expf(ep[0]), expf(ep[1]), expf(ep[2]));
     f3 em1 = mk3(expm1f(ep[0]), expm1f(ep[1]), expm1f(ep[2]));
+    f3 ee = mk3(1.f + em1.x, 1.f + em1.y, 1.f + em1.z);  // exp(ep), one rounding from expm1
     o.expe = ee;
     o.dm1 = em1;
     o.newF = usv(sv.U, ee, sv.V);
