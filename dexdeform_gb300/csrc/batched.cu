@@ -34,9 +34,8 @@ using namespace dexmpm;
 // Compile-time tuning knobs.  Defaults were picked by timing every kernel on
 // GB300 over the 64-env batch: minimum resident CTAs per SM (register caps:
 // P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint 128) and the unrolling
-// of the outer loop over the 27 stencil nodes (rolled where registers are
-// tight; fully unrolled in the fused kernel's gather and the G2P adjoint's
-// direct scatter, which keeps their weight arrays out of local memory).
+// of the outer loop over the 27 stencil nodes in the adjoints (full unrolling
+// keeps the weight arrays out of local memory).
 #ifndef DEX_P2G_MINB
 #define DEX_P2G_MINB 3
 #endif
@@ -52,22 +51,14 @@ using namespace dexmpm;
 #ifndef DEX_G2P_GRAD_UNROLL
 #define DEX_G2P_GRAD_UNROLL 3
 #endif
-#ifndef DEX_G2P2G_UNROLL
-#define DEX_G2P2G_UNROLL 3
-#endif
 #ifndef DEX_G2P_GRAD_MINB
 #define DEX_G2P_GRAD_MINB 3
-#endif
-#ifndef DEX_NODE_UNROLL
-#define DEX_NODE_UNROLL 1
 #endif
 // Scatter: warps with more than DEX_DIRECT_SEGS segments of equal stencil
 // base use per-lane atomics instead of the transposed reduction.
 #ifndef DEX_DIRECT_SEGS
 #define DEX_DIRECT_SEGS 8
 #endif
-constexpr int kNodeUnroll = DEX_NODE_UNROLL;
-constexpr int kG2p2gUnroll = DEX_G2P2G_UNROLL;
 constexpr int kG2pGradUnroll = DEX_G2P_GRAD_UNROLL;
 constexpr int kP2gGradUnroll = DEX_P2G_GRAD_UNROLL;
 
@@ -95,6 +86,12 @@ __device__ __forceinline__ m33 ldm33(const float *__restrict__ S, int N, int pla
 __device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m33 &m) {
 #pragma unroll
   for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
+}
+
+// L2 prefetch of the cache lines holding particles p0 .. p1 of one plane.
+__device__ __forceinline__ void prefetch_plane(const float *plane, int p0, int p1) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(plane + p0));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(plane + p1));
 }
 
 // SVD tape: the recomputed forward P2G stores each particle's SVD of F_tmp
@@ -168,6 +165,55 @@ __device__ __forceinline__ bool stencil_in_grid(const DexEnv &E, const Stencil &
          st.base[1] + 2 < E.gy && st.base[2] + 2 < E.gz;
 }
 
+// G2P gather of the grid velocities g_n of the 27 stencil nodes with weights
+// w_n = wx_i wy_j wz_k: s0 = sum w g and the offset moments si = sum i w g,
+// sj = sum j w g, sk = sum k w g, summed one axis at a time (z within a row,
+// then y, then x) so that no node needs its own weight product.  Lanes with
+// ok false read nothing and get zeros.
+struct Moments {
+  f3 s0, si, sj, sk;
+};
+__device__ __forceinline__ f3 xyz(float4 g) { return mk3(g.x, g.y, g.z); }
+__device__ __forceinline__ Moments gather_moments(const float4 *__restrict__ grid, const NodeCells &nc,
+                                                  const Stencil &st, bool ok) {
+  Moments o;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    f3 q, qj, qk;  // sums over the x-row i: w_y w_z g, j w_y w_z g, k w_y w_z g
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const f3 g0 = xyz(ok ? __ldg(grid + nc.at(i, j, 0)) : z4);
+      const f3 g1 = xyz(ok ? __ldg(grid + nc.at(i, j, 1)) : z4);
+      const f3 g2 = xyz(ok ? __ldg(grid + nc.at(i, j, 2)) : z4);
+      const f3 t1 = g1 * st.w[2][1];
+      const f3 pz = g0 * st.w[2][0] + t1 + g2 * st.w[2][2];  // sum_k w_z g
+      const f3 kz = t1 + g2 * (2.f * st.w[2][2]);           // sum_k k w_z g
+      const float wy = st.w[1][j];
+      if (j == 0) {
+        q = pz * wy;
+        qk = kz * wy;
+      } else {
+        q += pz * wy;
+        qk += kz * wy;
+        qj = j == 1 ? pz * wy : qj + pz * (2.f * wy);
+      }
+    }
+    const float wx = st.w[0][i];
+    if (i == 0) {
+      o.s0 = q * wx;
+      o.sj = qj * wx;
+      o.sk = qk * wx;
+    } else {
+      o.s0 += q * wx;
+      o.sj += qj * wx;
+      o.sk += qk * wx;
+      o.si = i == 1 ? q * wx : o.si + q * (2.f * wx);
+    }
+  }
+  return o;
+}
+
 __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, float d) {
   atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(a, b, c, d));
 }
@@ -184,11 +230,14 @@ __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, 
 // over each segment with plain loads, and the segment's total goes to the
 // grid in one 8-byte vector atomic.  Rows are padded to 132 floats so that the
 // loads (8 B per lane, one row per lane pair) are free of bank conflicts.
-// Warps with more than DEX_DIRECT_SEGS segments (about one particle per cell)
-// add their contributions with per-lane float4 atomics instead.
-constexpr int kRedRow = 132;                      // floats per node row (32 lanes x 4 + 4 pad)
-constexpr int kRedWarpFloats = 16 * kRedRow + 32;  // 16 node rows + the position table
+// The segment's target cells come from a per-warp table of its head lane's
+// per-axis cell terms (NodeCells), written once per warp.  Warps with more
+// than DEX_DIRECT_SEGS segments (about one particle per cell) add their
+// contributions with per-lane float4 atomics instead.
+constexpr int kRedRow = 132;  // floats per node row (32 lanes x 4 + 4 pad)
 constexpr int kDirectSegs = DEX_DIRECT_SEGS;
+constexpr int kSegTable = 16 * kRedRow;                      // after the 16 node rows
+constexpr int kRedWarpFloats = kSegTable + 9 * kDirectSegs;  // + 9 cell terms per segment
 constexpr size_t kScatterSmemPerWarp = sizeof(float) * kRedWarpFloats;
 
 __device__ __forceinline__ float *warp_red_buffer() {
@@ -200,12 +249,11 @@ __device__ __forceinline__ float *warp_red_buffer() {
 // structure of that order (key INT_MAX: no contribution, placed last).
 struct Ranked {
   int r;           // position of this lane
-  int src;         // lane at position `lane` (for per-segment lookups)
   unsigned heads;  // bit q: position q starts a segment of live lanes
   int n_live;      // live lanes occupy positions [0, n_live)
   bool head;       // this lane starts its segment
 };
-__device__ __forceinline__ Ranked rank_lanes(int key, int lane, float *red) {
+__device__ __forceinline__ Ranked rank_lanes(int key, int lane) {
   // Lanes with equal keys found in one match; segments are ordered by their
   // lowest lane, positions within a segment by lane, dead lanes (INT_MAX)
   // after all live ones.
@@ -227,12 +275,23 @@ __device__ __forceinline__ Ranked rank_lanes(int key, int lane, float *red) {
   R.r = (live ? seg0 : R.n_live) + within;
   R.head = lead && live;
   R.heads = __reduce_or_sync(kFull, R.head ? (1u << seg0) : 0u);
-  int *pos = reinterpret_cast<int *>(red + 16 * kRedRow);
-  pos[R.r] = lane;
-  __syncwarp();
-  R.src = pos[lane];
-  __syncwarp();
   return R;
+}
+
+// Head lanes of the first kDirectSegs segments store their cell terms in the
+// warp's segment table (entry = segment ordinal); a __syncwarp must follow
+// before red_walk reads it.
+__device__ __forceinline__ void put_segment(float *red, const Ranked &R, const NodeCells &nc) {
+  const int sidx = __popc(R.heads & ((1u << R.r) - 1u));
+  if (R.head && sidx < kDirectSegs) {
+    int *t = reinterpret_cast<int *>(red + kSegTable) + 9 * sidx;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      t[d] = nc.x[d];
+      t[3 + d] = nc.y[d];
+      t[6 + d] = nc.z[d];
+    }
+  }
 }
 
 __device__ __forceinline__ void red_put(float *red, int c, int pos, float a, float b, float d, float e) {
@@ -240,24 +299,21 @@ __device__ __forceinline__ void red_put(float *red, int c, int pos, float a, flo
 }
 
 // Sum the stored rows of nodes node0 .. node0 + n_nodes - 1 over every segment
-// of positions and add them at the segment's stencil base + node offset (base:
-// each lane's own particle's base).  Warp-uniform.
-__device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int node0, int n_nodes, const int base[3],
-                                         const DexEnv &E, float *grid, int lane) {
+// of positions and add them at the segment's stencil nodes (cell terms from
+// the segment table).  Warp-uniform; at most kDirectSegs segments.
+__device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int node0, int n_nodes, float *grid,
+                                         int lane) {
   const int c = lane >> 1, h = lane & 1;
-  const int n = node0 + c;
   const bool act = c < n_nodes;
+  const int n = act ? node0 + c : 0;
   const int ni = n / 9, nj = (n / 3) % 3, nk = n % 3;
   const float *col = red + c * kRedRow + 2 * h;
+  const int *tab = reinterpret_cast<const int *>(red + kSegTable);
   unsigned rest = R.heads;
-  while (rest) {
+  for (int sidx = 0; rest; ++sidx) {
     const int start = __ffs(rest) - 1;
     rest &= rest - 1u;
     const int end = rest ? __ffs(rest) - 1 : R.n_live;
-    const int owner = __shfl_sync(kFull, R.src, start);
-    const int bx = __shfl_sync(kFull, base[0], owner);
-    const int by = __shfl_sync(kFull, base[1], owner);
-    const int bz = __shfl_sync(kFull, base[2], owner);
     float2 acc = make_float2(0.f, 0.f);
     for (int q = start; q < end; ++q) {
       const float2 t = *reinterpret_cast<const float2 *>(col + 4 * q);
@@ -265,7 +321,8 @@ __device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int 
       acc.y += t.y;
     }
     if (act) {
-      const int ci = cell_index(E, bx + ni, by + nj, bz + nk);
+      const int *t = tab + 9 * sidx;
+      const int ci = t[ni] + t[3 + nj] + t[6 + nk];
       atomicAdd(reinterpret_cast<float2 *>(grid + 4 * (size_t)ci + 2 * h), acc);
     }
   }
@@ -369,7 +426,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
   }
   if (!live) st.base[0] = st.base[1] = st.base[2] = 0;
   float *red = warp_red_buffer();
-  const Ranked R = rank_lanes(key, lane, red);
+  const Ranked R = rank_lanes(key, lane);
 
   const float m = live ? __ldg(B.mass + p) : 0.f;
   const float vol = __ldg(B.vol + p);
@@ -409,6 +466,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
           }
         }
   } else {
+    if (R.head) put_segment(red, R, node_cells(E, st.base));
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
 #pragma unroll
@@ -422,7 +480,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
         }
       }
       __syncwarp();
-      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, st.base, E, grid, lane);
+      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, grid, lane);
       __syncwarp();
     }
   }
@@ -476,32 +534,17 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
   const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, Xg));
   // v = sum w v_n;  C = 4 inv_dx sum w v_n ((i, j, k) - fx)^T
-  //   = 4 inv_dx (sum w v_n (i, j, k)^T - v fx^T), the node offsets being
-  //   constants of the unrolled loops
-  f3 nv = mk3(0.f, 0.f, 0.f), ci = mk3(0.f, 0.f, 0.f), cj = mk3(0.f, 0.f, 0.f), ck = mk3(0.f, 0.f, 0.f);
-#pragma unroll kG2p2gUnroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g = ok ? __ldg(vout + nc.at(i, j, k))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-        const f3 a = mk3(g.x, g.y, g.z) * w;
-        nv += a;
-        if (i) ci += i == 1 ? a : a * 2.f;
-        if (j) cj += j == 1 ? a : a * 2.f;
-        if (k) ck += k == 1 ? a : a * 2.f;
-      }
+  //   = 4 inv_dx (sum w v_n (i, j, k)^T - v fx^T)
+  const Moments mo = gather_moments(vout, nc, st, ok);
+  const f3 nv = mo.s0;
   const float c4 = 4.f * E.inv_dx;
+  const f3 col[3] = {mo.si - nv * st.fx[0], mo.sj - nv * st.fx[1], mo.sk - nv * st.fx[2]};
   m33 nC;
-  const f3 col[3] = {ci - nv * st.fx[0], cj - nv * st.fx[1], ck - nv * st.fx[2]};
 #pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    nC.a[r][0] = (r == 0 ? col[0].x : r == 1 ? col[0].y : col[0].z) * c4;
-    nC.a[r][1] = (r == 0 ? col[1].x : r == 1 ? col[1].y : col[1].z) * c4;
-    nC.a[r][2] = (r == 0 ? col[2].x : r == 1 ? col[2].y : col[2].z) * c4;
+  for (int c = 0; c < 3; ++c) {
+    nC.a[0][c] = col[c].x * c4;
+    nC.a[1][c] = col[c].y * c4;
+    nC.a[2][c] = col[c].z * c4;
   }
   f3 nx = x + nv * E.dt;
   const float lo = E.ground_height * E.dx;
@@ -583,7 +626,7 @@ __global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, int Y, const
 
 // =================================================================== G2P
 // integrator.cu:1059-1109.
-__global__ void __launch_bounds__(256) k_g2p(DexBatch B, int X, const float *__restrict__ S,
+__global__ void __launch_bounds__(256, 3) k_g2p(DexBatch B, int X, const float *__restrict__ S,
                                              float *__restrict__ Snext) {
   const int tile = blockIdx.x;
   const DexEnv E = B.envs[B.tiles[2 * tile]];
@@ -598,22 +641,18 @@ __global__ void __launch_bounds__(256) k_g2p(DexBatch B, int X, const float *__r
   if (!stencil_in_grid(E, st)) return;  // reported by P2G
   const NodeCells nc = node_cells(E, st.base);
   const float4 *__restrict__ vout = reinterpret_cast<const float4 *>(slot_vout(B, X));
-  f3 nv = mk3(0.f, 0.f, 0.f);
-  m33 nC = mzero();
+  // v = sum w v_n;  C = 4 inv_dx sum w v_n ((i, j, k) - fx)^T
+  const Moments mo = gather_moments(vout, nc, st, true);
+  const f3 nv = mo.s0;
   const float c4 = 4.f * E.inv_dx;
-#pragma unroll kNodeUnroll
-  for (int i = 0; i < 3; ++i)
+  const f3 col[3] = {mo.si - nv * st.fx[0], mo.sj - nv * st.fx[1], mo.sk - nv * st.fx[2]};
+  m33 nC;
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float w = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g = __ldg(vout + nc.at(i, j, k));
-        const f3 gv = mk3(g.x, g.y, g.z);
-        const f3 dpos = mk3((float)i - st.fx[0], (float)j - st.fx[1], (float)k - st.fx[2]);
-        nv += gv * w;
-        nC += outer(gv, dpos) * (w * c4);
-      }
+  for (int c = 0; c < 3; ++c) {
+    nC.a[0][c] = col[c].x * c4;
+    nC.a[1][c] = col[c].y * c4;
+    nC.a[2][c] = col[c].z * c4;
+  }
   f3 nx = x + nv * E.dt;
   const float lo = E.ground_height * E.dx;
   nx.x = fmaxf(fminf(nx.x, (E.gx - 3.f) * E.dx), lo);
@@ -649,7 +688,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   const bool live = key != INT_MAX;
   if (!live) st.base[0] = st.base[1] = st.base[2] = 0;
   float *red = warp_red_buffer();
-  const Ranked R = rank_lanes(key, lane, red);
+  const Ranked R = rank_lanes(key, lane);
   f3 gx = ldf3(Gnext, N, PX, p);
   f3 gnv = ldf3(Gnext, N, PV, p);
   const m33 gC = live ? ldm33(Gnext, N, PC, p) : mzero();
@@ -697,6 +736,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
           if (live) red_add4(vg + 4 * (size_t)ci, ggv.x, ggv.y, ggv.z, 0.f);
         }
   } else {
+    put_segment(red, R, nc);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
 #pragma unroll
@@ -710,7 +750,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
         }
       }
       __syncwarp();
-      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, st.base, E, vg, lane);
+      red_walk(red, R, 16 * g, g == 0 ? 16 : 11, vg, lane);
       __syncwarp();
     }
   }
@@ -847,8 +887,26 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   const DexEnv E = B.envs[B.tiles[2 * tile]];
   const int first = B.tiles[2 * tile + 1];
   const int loc = first + part * blockDim.x + threadIdx.x;
-  if (loc >= E.n) return;
   const int N = B.n_particles;
+  if constexpr (kTape) {
+    // the 48 planes read after the gather (F, material, SVD, incoming F and x
+    // gradients) for this warp's particles, one plane per lane, into L2
+    const int w0 = first + part * blockDim.x + (threadIdx.x & ~31);
+    if (w0 < E.n) {
+      const int p0 = E.p_off + w0, p1 = E.p_off + min(w0 + 31, E.n - 1);
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int q = lane; q < 48; q += 32) {
+        const float *pl = q < 9    ? S + (size_t)(PF + q) * N
+                          : q < 12 ? B.mu_lam_yield + (size_t)(q - 9) * N
+                          : q < 36 ? tape + (size_t)(q - 12) * N
+                          : q < 45 ? Gnext + (size_t)(PF + q - 36) * N
+                                   : G + (size_t)(q - 45) * N;
+        prefetch_plane(pl, p0, p1);
+      }
+    }
+  }
+  if (loc >= E.n) return;
   const int p = E.p_off + loc;
   const f3 x = ldf3(S, N, PX, p);
   Stencil st;
