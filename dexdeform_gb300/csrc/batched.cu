@@ -135,14 +135,11 @@ __device__ __forceinline__ int32_t *slot_list(const DexBatch &B, int k) {
   return B.block_list + (size_t)k * B.n_blocks;
 }
 
-__device__ __forceinline__ int cell_index(const DexEnv &E, int x, int y, int z) {
-  int nby = E.gy >> 2, nbz = E.gz >> 2;
-  int blk = E.blk_off + ((x >> 2) * nby + (y >> 2)) * nbz + (z >> 2);
-  return (blk << 6) + ((x & 3) << 4) + ((y & 3) << 2) + (z & 3);
-}
 
-// Cell indices of the 27 stencil nodes as sums of per-axis terms:
-// cell_index(E, b0 + i, b1 + j, b2 + k) = x[i] + y[j] + z[k].
+// Grid cells are stored in 4^3 blocks of 64 float4 cells: cell (x, y, z) of an
+// env is entry ((blk_off + (x/4 * nby + y/4) * nbz + z/4) * 64 + (x%4) * 16 +
+// (y%4) * 4 + z%4), nby = gy/4, nbz = gz/4.  The 27 stencil nodes of base
+// (b0, b1, b2) are then x[i] + y[j] + z[k] with per-axis terms.
 struct NodeCells {
   int x[3], y[3], z[3];
   __device__ __forceinline__ int at(int i, int j, int k) const { return x[i] + y[j] + z[k]; }
@@ -1124,6 +1121,13 @@ int scatter_attr_ready() {
 }
 bool grad_ok(const DexBatch *b) { return valid(b) && b->vout_grad && b->in_grad; }
 
+// Kernel launch on the caller's stream; returns the launch status.
+template <typename... P, typename... A>
+int launch(void (*kernel)(P...), int grid, int block, size_t smem, dexmpm_stream_t stream, A... args) {
+  kernel<<<grid, block, smem, (cudaStream_t)stream>>>(args...);
+  return check_launch();
+}
+
 }  // namespace
 
 extern "C" {
@@ -1149,8 +1153,7 @@ int dexmpm_p2g(const DexBatch *b, int slot, const float *S, float *Snext, float 
   if (!valid(b) || !S || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   if (int rc = scatter_attr_ready()) return rc;
-  k_p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext, tape);
-  return check_launch();
+  return launch(k_p2g, b->n_tiles, b->tile_size, scatter_smem(b->tile_size), stream, *b, slot, S, Snext, tape);
 }
 
 int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pose, const float *next_pose,
@@ -1158,16 +1161,14 @@ int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pos
   if (!valid(b) || !slot_ok(b, slot) || (clear_slot >= 0 && (!slot_ok(b, clear_slot) || clear_slot == slot)))
     return DEXMPM_ERR_ARG;
   if (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape)) return DEXMPM_ERR_ARG;
-  k_grid_op<<<grid_ctas(b, (const void *)k_grid_op, kGridOp), 256, 0, (cudaStream_t)stream>>>(
-      *b, slot, clear_slot < 0 ? -1 : clear_slot, pose, next_pose);
-  return check_launch();
+  return launch(k_grid_op, grid_ctas(b, (const void *)k_grid_op, kGridOp), 256, 0, stream, *b, slot,
+                clear_slot < 0 ? -1 : clear_slot, pose, next_pose);
 }
 
 int dexmpm_g2p(const DexBatch *b, int slot, const float *S, float *Snext, dexmpm_stream_t stream) {
   if (!valid(b) || !S || !Snext || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
-  k_g2p<<<b->n_tiles, b->tile_size, 0, (cudaStream_t)stream>>>(*b, slot, S, Snext);
-  return check_launch();
+  return launch(k_g2p, b->n_tiles, b->tile_size, 0, stream, *b, slot, S, Snext);
 }
 
 int dexmpm_g2p2g(const DexBatch *b, int slot_g, int slot_s, const float *S, float *Snext, float *S2, float *tape,
@@ -1177,9 +1178,8 @@ int dexmpm_g2p2g(const DexBatch *b, int slot_g, int slot_s, const float *S, floa
     return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   if (int rc = scatter_attr_ready()) return rc;
-  k_g2p2g<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot_g, slot_s, S, Snext,
-                                                                                        S2, tape);
-  return check_launch();
+  return launch(k_g2p2g, b->n_tiles, b->tile_size, scatter_smem(b->tile_size), stream, *b, slot_g, slot_s, S, Snext,
+                S2, tape);
 }
 
 int dexmpm_substep(const DexBatch *b, int slot, int clear_slot, const float *S, float *Snext, const float *pose,
@@ -1196,18 +1196,16 @@ int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *S, const float *Sn
   if (!grad_ok(b) || !S || !Snext || !Gnext || !G || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_tiles == 0) return DEXMPM_OK;
   if (int rc = scatter_attr_ready()) return rc;
-  k_g2p_grad<<<b->n_tiles, b->tile_size, scatter_smem(b->tile_size), (cudaStream_t)stream>>>(*b, slot, S, Snext, Gnext,
-                                                                                           G);
-  return check_launch();
+  return launch(k_g2p_grad, b->n_tiles, b->tile_size, scatter_smem(b->tile_size), stream, *b, slot, S, Snext, Gnext,
+                G);
 }
 
 int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const float *next_pose, float *bgrad,
                         float *next_bgrad, dexmpm_stream_t stream) {
   if (!grad_ok(b) || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
   if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape)) return DEXMPM_ERR_ARG;
-  k_grid_op_grad<<<grid_ctas(b, (const void *)k_grid_op_grad, kGridOpGrad), 256, 0, (cudaStream_t)stream>>>(
-      *b, slot, pose, next_pose, bgrad, next_bgrad);
-  return check_launch();
+  return launch(k_grid_op_grad, grid_ctas(b, (const void *)k_grid_op_grad, kGridOpGrad), 256, 0, stream, *b, slot,
+                pose, next_pose, bgrad, next_bgrad);
 }
 
 int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gnext, float *G, const float *tape,
@@ -1217,11 +1215,9 @@ int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gn
   // the adjoint is register-heavy: 128-thread CTAs, tile_size/128 of them per tile
   const int cta = b->tile_size < 128 ? b->tile_size : 128;
   const int split = b->tile_size / cta;
-  if (tape)
-    k_p2g_grad<true><<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split, tape);
-  else
-    k_p2g_grad<false><<<b->n_tiles * split, cta, 0, (cudaStream_t)stream>>>(*b, slot, S, Gnext, G, split, nullptr);
-  return check_launch();
+  if (tape) return launch(k_p2g_grad<true>, b->n_tiles * split, cta, 0, stream, *b, slot, S, Gnext, G, split, tape);
+  return launch(k_p2g_grad<false>, b->n_tiles * split, cta, 0, stream, *b, slot, S, Gnext, G, split,
+                (const float *)nullptr);
 }
 
 int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float *Snext, const float *Gnext,
@@ -1237,9 +1233,8 @@ int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float
 int dexmpm_clear_slots(const DexBatch *b, int first, int last, dexmpm_stream_t stream) {
   if (!valid(b) || first < 0 || last > b->n_slots || first > last) return DEXMPM_ERR_ARG;
   if (first == last) return DEXMPM_OK;
-  k_clear_slots<<<grid_ctas(b, (const void *)k_clear_slots, kClearSlots), 256, 0, (cudaStream_t)stream>>>(*b, first,
-                                                                                                   last);
-  return check_launch();
+  return launch(k_clear_slots, grid_ctas(b, (const void *)k_clear_slots, kClearSlots), 256, 0, stream, *b, first,
+                last);
 }
 
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream) {
