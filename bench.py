@@ -384,20 +384,28 @@ def kernel_times(E, R, s0, g_final):
     pass_([ck[0]] + [ring[t] for t in range(1, T + 1)], kept=True)    # recompute of the backward
     torch.cuda.synchronize()
     cells = float(E.block_count[2:2 + T].double().mean()) * 64  # active cells per substep
+    # the adjoint as BatchEngine.run_adjoint runs it: G2P adjoint of the last
+    # substep, then per substep the grid adjoint and the P2G adjoint, fused
+    # with the previous substep's G2P adjoint for all but the first
     gn, g = R.gbuf[1], R.gbuf[0]
     gn.copy_(g_final)
+    sts = [ck[0]] + [ring[t] for t in range(1, T + 1)]
+    timed("g2p_grad", lambda: N.check(L.dexmpm_g2p_grad(E._bp, 1 + T, N.ptr(sts[T - 1]), N.ptr(sts[T]), N.ptr(gn),
+                                                        N.ptr(g), sp), "g2p_grad"))
     for s in range(T - 1, -1, -1):
         slot = 2 + s
-        cur = ck[0] if s == 0 else ring[s]
-        nxt = ring[s + 1]
         pz, pn = R.poses[s], R.poses[s + 1]
-        timed("g2p_grad", lambda: N.check(L.dexmpm_g2p_grad(E._bp, slot, N.ptr(cur), N.ptr(nxt), N.ptr(gn), N.ptr(g),
-                                                            sp), "g2p_grad"))
         timed("grid_op_grad", lambda: N.check(L.dexmpm_grid_op_grad(E._bp, slot, N.ptr(pz), N.ptr(pn),
                                                                     N.ptr(R.bgrad[s]), N.ptr(R.bgrad[s + 1]), sp),
                                               "grid_op_grad"))
-        timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, slot, N.ptr(cur), N.ptr(gn), N.ptr(g),
-                                                            N.ptr(R._tape(s)), sp), "p2g_grad"))
+        if s > 0:
+            timed("p2g2g_grad", lambda: N.check(L.dexmpm_p2g_g2p_grad(E._bp, slot, slot - 1, N.ptr(sts[s]),
+                                                                      N.ptr(sts[s - 1]), N.ptr(gn), N.ptr(g),
+                                                                      N.ptr(gn), N.ptr(R._tape(s)), sp),
+                                                "p2g2g_grad"))
+        else:
+            timed("p2g_grad", lambda: N.check(L.dexmpm_p2g_grad(E._bp, slot, N.ptr(sts[0]), N.ptr(gn), N.ptr(g),
+                                                                N.ptr(R._tape(0)), sp), "p2g_grad"))
         gn, g = g, gn
     torch.cuda.synchronize()
     return {k: 1e3 * sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in acc.items()}, cells
@@ -416,6 +424,8 @@ ALG_BYTES = {
     "g2p_grad": (96, 32),      # x, v', dL/d(x v C)' read, dL/dx written; v_out read, dL/dv_out scattered
     "grid_op_grad": (0, 80),   # (mv, m), dL/dv_out read, dL/d(mv, m) written, dL/dv_out and the slot zeroed
     "p2g_grad": (392, 16),     # x v F C + material + tape + dL/dF', dL/dx read, dL/d(x v F C) written; dL/d(mv,m) gathered
+    "p2g2g_grad": (356, 48),   # p2g_grad's reads, dL/dF written; x of the previous state read, its dL/dx written;
+                               # dL/d(mv,m) and v_out gathered, dL/dv_out scattered
 }
 
 
@@ -428,7 +438,8 @@ NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
 def launches_per_substep(T):
     return {"p2g": 1 / T, "p2g_tape": 1 / T, "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1,
-            "grid_op_keep": 1, "g2p": 2 / T, "g2p_grad": 1, "grid_op_grad": 1, "p2g_grad": 1}
+            "grid_op_keep": 1, "g2p": 2 / T, "g2p_grad": 1 / T, "grid_op_grad": 1, "p2g_grad": 1 / T,
+            "p2g2g_grad": 1 - 1 / T}
 
 
 def roofline(E, kt, cells):

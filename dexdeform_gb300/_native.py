@@ -71,6 +71,7 @@ _BATCH_SIGS = {
     "dexmpm_g2p_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
     "dexmpm_grid_op_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
     "dexmpm_p2g_grad": [POINTER(DexBatch), c_int, P, P, P, P, P],
+    "dexmpm_p2g_g2p_grad": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P, P, P],
     "dexmpm_get_error": [POINTER(DexBatch), POINTER(c_int32), P],
     "dexmpm_substep_noalloc": [POINTER(DexEnv), P, P, P, P, P, P, P, P, P, P],
     "dexmpm_abi_get_error": [POINTER(c_int32)],

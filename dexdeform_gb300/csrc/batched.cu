@@ -661,22 +661,18 @@ __global__ void __launch_bounds__(256, 3) k_g2p(DexBatch B, int X, const float *
 }
 
 // ============================================================ G2P adjoint
-// integrator.cu:1527-1614.  Writes (not adds) the x gradient of state s.
-__global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B, int X, const float *__restrict__ S,
-                                                  const float *__restrict__ Snext, const float *__restrict__ Gnext,
-                                                  float *__restrict__ G) {
-  const int tile = blockIdx.x;
-  const DexEnv E = B.envs[B.tiles[2 * tile]];
-  const int first = B.tiles[2 * tile + 1];
+// integrator.cu:1527-1614 for the particle of this lane: from its position x
+// in state s, its velocity vnext in state s + 1 and the incoming gradients of
+// state s + 1 (gx, gnv, gC), scatters dL/dv_out into the adjoint grid and
+// writes (not adds) the x gradient of state s to G.  Every lane of the warp
+// calls it; `in`: the lane has a particle.
+__device__ __forceinline__ void g2p_grad_lane(const DexBatch &B, const DexEnv &E, int X, int p, bool in, f3 x,
+                                              f3 vnext, f3 gx, f3 gnv, m33 gC, float *G, int lane) {
   const int N = B.n_particles;
-  const int lane = threadIdx.x & 31;
-  const int loc = first + threadIdx.x;
-  const int p = E.p_off + (loc < E.n ? loc : 0);
-  const f3 x = ldf3(S, N, PX, p);
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   int key = INT_MAX;
-  if (loc < E.n) {
+  if (in) {
     if (stencil_in_grid(E, st))
       key = (st.base[0] * E.gy + st.base[1]) * E.gz + st.base[2];
     else
@@ -686,10 +682,8 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   if (!live) st.base[0] = st.base[1] = st.base[2] = 0;
   float *red = warp_red_buffer();
   const Ranked R = rank_lanes(key, lane);
-  f3 gx = ldf3(Gnext, N, PX, p);
-  f3 gnv = ldf3(Gnext, N, PV, p);
-  const m33 gC = live ? ldm33(Gnext, N, PC, p) : mzero();
-  const f3 nx = x + ldf3(Snext, N, PV, p) * E.dt;
+  if (!live) gC = mzero();
+  const f3 nx = x + vnext * E.dt;
   const float lo = E.ground_height * E.dx;
   if (nx.x > (E.gx - 3.f) * E.dx || nx.x < lo) gx.x = 0.f;
   if (nx.y > (E.gy - 3.f) * E.dx || nx.y < lo) gx.y = 0.f;
@@ -754,6 +748,23 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
   // the C-gradient term of every node: sum_n gC^T v_n (-inv_dx c4 w_n)
   gx += mtv(gC, wgv) * (-E.inv_dx * c4);
   if (live) stf3(G, N, PX, p, gx);
+}
+
+// G2P adjoint of substep s: x of state s from S, v of state s + 1 from Snext,
+// the gradients of state s + 1 from Gnext; the x gradient of state s to G.
+__global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B, int X, const float *__restrict__ S,
+                                                  const float *__restrict__ Snext, const float *__restrict__ Gnext,
+                                                  float *__restrict__ G) {
+  const int tile = blockIdx.x;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  const int loc = first + threadIdx.x;
+  const bool in = loc < E.n;
+  const int p = E.p_off + (in ? loc : 0);
+  g2p_grad_lane(B, E, X, p, in, ldf3(S, N, PX, p), ldf3(Snext, N, PV, p), ldf3(Gnext, N, PX, p),
+                ldf3(Gnext, N, PV, p), ldm33(Gnext, N, PC, p), G, lane);
 }
 
 // ===================================================== grid update adjoint
@@ -871,45 +882,20 @@ __global__ void __launch_bounds__(256, 3) k_grid_op_grad(DexBatch B, int X, cons
 }
 
 // ============================================================ P2G adjoint
-
-// integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad).
-// Adds to the x gradient written by k_g2p_grad and writes v, F, C gradients.
-// With kTape the SVD of F_tmp comes from the tape the recomputed forward
-// wrote (same values, without the SVD's registers and arithmetic).
+// integrator.cu:396-627 (p2g_grad) fused with :110-186 (compute_svd_grad) for
+// particle p at x (stencil st inside the grid): the gradients of its state s
+// (x: the part from the G2P adjoint, read from G, plus this part; v, F, C) from the
+// adjoint grid of slot X (dL/d(mv, m), in in_grad) and the incoming F
+// gradient of state s + 1.  With kTape the SVD and stress of F_tmp come from
+// the tape the recomputed forward wrote (same values, without the SVD's
+// registers and arithmetic).  v: the particle's velocity in state s.
 template <bool kTape>
-__global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
-                                                  const float *__restrict__ Gnext, float *__restrict__ G,
-                                                  int split, const float *__restrict__ tape) {
-  const int tile = blockIdx.x / split, part = blockIdx.x % split;
-  const DexEnv E = B.envs[B.tiles[2 * tile]];
-  const int first = B.tiles[2 * tile + 1];
-  const int loc = first + part * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEnv &E, int p, const Stencil &st,
+                                                  const float *__restrict__ S, const float *__restrict__ Gnext,
+                                                  const float *G, const float *__restrict__ tape, f3 &v, f3 &o_gx,
+                                                  f3 &o_gv, m33 &o_gF, m33 &o_gC) {
   const int N = B.n_particles;
-  if constexpr (kTape) {
-    // the 48 planes read after the gather (F, material, SVD, incoming F and x
-    // gradients) for this warp's particles, one plane per lane, into L2
-    const int w0 = first + part * blockDim.x + (threadIdx.x & ~31);
-    if (w0 < E.n) {
-      const int p0 = E.p_off + w0, p1 = E.p_off + min(w0 + 31, E.n - 1);
-      const int lane = threadIdx.x & 31;
-#pragma unroll
-      for (int q = lane; q < 48; q += 32) {
-        const float *pl = q < 9    ? S + (size_t)(PF + q) * N
-                          : q < 12 ? B.mu_lam_yield + (size_t)(q - 9) * N
-                          : q < 36 ? tape + (size_t)(q - 12) * N
-                          : q < 45 ? Gnext + (size_t)(PF + q - 36) * N
-                                   : G + (size_t)(q - 45) * N;
-        prefetch_plane(pl, p0, p1);
-      }
-    }
-  }
-  if (loc >= E.n) return;
-  const int p = E.p_off + loc;
-  const f3 x = ldf3(S, N, PX, p);
-  Stencil st;
-  make_stencil(x, E.inv_dx, st);
-  if (!stencil_in_grid(E, st)) return;
-  const f3 v = ldf3(S, N, PV, p);
+  v = ldf3(S, N, PV, p);
   const m33 C = ldm33(S, N, PC, p);
   const float m = __ldg(B.mass + p), vol = __ldg(B.vol + p);
   const float gss = -E.dt * E.inv_dx * vol * 4.f * E.inv_dx;
@@ -1023,11 +1009,107 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
   m33 IdtC = C * E.dt;
   IdtC.a[0][0] += 1.f; IdtC.a[1][1] += 1.f; IdtC.a[2][2] += 1.f;
   const m33 gF = mm(mT(IdtC), Gt);
-  const f3 gx0 = mk3(G[p], G[(size_t)N + p], G[(size_t)2 * N + p]);
-  stf3(G, N, PX, p, gx0 + g_x);
-  stf3(G, N, PV, p, g_v);
+  o_gx = ldf3(G, N, PX, p) + g_x;
+  o_gv = g_v;
+  o_gF = gF;
+  o_gC = gC_total;
+}
+
+// P2G adjoint of substep s: adds to the x gradient written by k_g2p_grad and
+// writes the v, F, C gradients of state s (G); 128-thread CTAs, `split` per tile.
+template <bool kTape>
+__global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B, int X, const float *__restrict__ S,
+                                                  const float *__restrict__ Gnext, float *__restrict__ G,
+                                                  int split, const float *__restrict__ tape) {
+  const int tile = blockIdx.x / split, part = blockIdx.x % split;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int loc = first + part * blockDim.x + threadIdx.x;
+  const int N = B.n_particles;
+  if constexpr (kTape) {
+    // the 48 planes read after the gather (F, material, SVD, incoming F and x
+    // gradients) for this warp's particles, one plane per lane, into L2
+    const int w0 = first + part * blockDim.x + (threadIdx.x & ~31);
+    if (w0 < E.n) {
+      const int p0 = E.p_off + w0, p1 = E.p_off + min(w0 + 31, E.n - 1);
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int q = lane; q < 48; q += 32) {
+        const float *pl = q < 9    ? S + (size_t)(PF + q) * N
+                          : q < 12 ? B.mu_lam_yield + (size_t)(q - 9) * N
+                          : q < 36 ? tape + (size_t)(q - 12) * N
+                          : q < 45 ? Gnext + (size_t)(PF + q - 36) * N
+                                   : G + (size_t)(q - 45) * N;
+        prefetch_plane(pl, p0, p1);
+      }
+    }
+  }
+  if (loc >= E.n) return;
+  const int p = E.p_off + loc;
+  const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  if (!stencil_in_grid(E, st)) return;
+  f3 v, gx, gv;
+  m33 gF, gC;
+  p2g_grad_particle<kTape>(B, E, p, st, S, Gnext, G, tape, v, gx, gv, gF, gC);
+  stf3(G, N, PX, p, gx);
+  stf3(G, N, PV, p, gv);
   stm33(G, N, PF, p, gF);
-  stm33(G, N, PC, p, gC_total);
+  stm33(G, N, PC, p, gC);
+}
+
+// P2G adjoint of substep s fused with the G2P adjoint of substep s - 1 for
+// the same particle (the adjoint counterpart of k_g2p2g).  The gradients of
+// state s stay in registers between the two: only its F gradient goes to G
+// (read by the P2G adjoint of substep s - 1); the G2P adjoint of substep s - 1
+// scatters into the adjoint grid and writes the x gradient of state s - 1 to
+// Gprev.  S: state s, Sprev: state s - 1, Gnext: gradients of state s + 1 (F
+// read), G: gradients of state s (x read: the part from the G2P adjoint of
+// substep s; F written).  Gprev may be Gnext (different planes).
+template <bool kTape>
+__global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g2g_grad(DexBatch B, int X, int Xprev, const float *S,
+                                                    const float *Sprev, const float *Gnext, float *G, float *Gprev,
+                                                    int split, const float *__restrict__ tape) {
+  const int tile = blockIdx.x / split, part = blockIdx.x % split;
+  const DexEnv E = B.envs[B.tiles[2 * tile]];
+  const int first = B.tiles[2 * tile + 1];
+  const int loc = first + part * blockDim.x + threadIdx.x;
+  const int N = B.n_particles;
+  const int lane = threadIdx.x & 31;
+  if constexpr (kTape) {
+    // as in k_p2g_grad: the planes read after the gather, into L2
+    const int w0 = first + part * blockDim.x + (threadIdx.x & ~31);
+    if (w0 < E.n) {
+      const int p0 = E.p_off + w0, p1 = E.p_off + min(w0 + 31, E.n - 1);
+#pragma unroll
+      for (int q = lane; q < 48; q += 32) {
+        const float *pl = q < 9    ? S + (size_t)(PF + q) * N
+                          : q < 12 ? B.mu_lam_yield + (size_t)(q - 9) * N
+                          : q < 36 ? tape + (size_t)(q - 12) * N
+                          : q < 45 ? Gnext + (size_t)(PF + q - 36) * N
+                                   : G + (size_t)(q - 45) * N;
+        prefetch_plane(pl, p0, p1);
+      }
+    }
+  }
+  const bool in = loc < E.n;
+  const int p = E.p_off + (in ? loc : 0);
+  const f3 x = ldf3(S, N, PX, p);
+  Stencil st;
+  make_stencil(x, E.inv_dx, st);
+  const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by the G2P adjoint
+  if (!ok) st.base[0] = st.base[1] = st.base[2] = 0;
+  f3 v, gx, gv;
+  m33 gF, gC;
+  p2g_grad_particle<kTape>(B, E, p, st, S, Gnext, G, tape, v, gx, gv, gF, gC);
+  if (ok) {
+    stm33(G, N, PF, p, gF);
+  } else {
+    gx = gv = mk3(0.f, 0.f, 0.f);
+    gC = mzero();
+  }
+  g2p_grad_lane(B, E, Xprev, p, in, ldf3(Sprev, N, PX, p), v, gx, gv, gC, Gprev, lane);
 }
 
 // Zero the grid cells and flags of the listed blocks of slots [first, last)
@@ -1218,6 +1300,21 @@ int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *S, const float *Gn
   if (tape) return launch(k_p2g_grad<true>, b->n_tiles * split, cta, 0, stream, *b, slot, S, Gnext, G, split, tape);
   return launch(k_p2g_grad<false>, b->n_tiles * split, cta, 0, stream, *b, slot, S, Gnext, G, split,
                 (const float *)nullptr);
+}
+
+int dexmpm_p2g_g2p_grad(const DexBatch *b, int slot, int prev_slot, const float *S, const float *Sprev,
+                        const float *Gnext, float *G, float *Gprev, const float *tape, dexmpm_stream_t stream) {
+  if (!grad_ok(b) || !S || !Sprev || !Gnext || !G || !Gprev || G == Gnext || G == Gprev || !slot_ok(b, slot) ||
+      !slot_ok(b, prev_slot) || slot == prev_slot)
+    return DEXMPM_ERR_ARG;
+  if (b->n_tiles == 0) return DEXMPM_OK;
+  const int cta = b->tile_size < 128 ? b->tile_size : 128;
+  const int split = b->tile_size / cta;
+  if (tape)
+    return launch(k_p2g2g_grad<true>, b->n_tiles * split, cta, scatter_smem(cta), stream, *b, slot, prev_slot, S,
+                  Sprev, Gnext, G, Gprev, split, tape);
+  return launch(k_p2g2g_grad<false>, b->n_tiles * split, cta, scatter_smem(cta), stream, *b, slot, prev_slot, S, Sprev,
+                Gnext, G, Gprev, split, (const float *)nullptr);
 }
 
 int dexmpm_substep_grad(const DexBatch *b, int slot, const float *S, const float *Snext, const float *Gnext,

@@ -312,6 +312,41 @@ class BatchEngine:
                 "dexmpm_substep_grad")
         self.launches += 3
 
+    def run_adjoint(self, sts: Sequence[torch.Tensor], g_next: torch.Tensor, g: torch.Tensor, poses: torch.Tensor,
+                    bgrad: torch.Tensor, tapes: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Adjoint of the T = len(sts) - 1 substeps that run_substeps(kept=True)
+        ran from sts[0] (grid slots 2..T+1, tapes[t] when given), from the
+        gradient of sts[T] in g_next; g is scratch of the same shape.  The P2G
+        adjoint of every substep but the first is fused with the G2P adjoint
+        of the substep before it.  Returns the buffer (g_next or g) that holds
+        the gradient of sts[0]; body-pose gradients of poses[t] are added to
+        bgrad[t].  Clears the slots."""
+        assert self.grad, "engine built without gradient buffers"
+        T = len(sts) - 1
+        assert T >= 1 and 2 + T <= self.n_grid_slots
+        L, bp, sp = self.lib, self._bp, N.stream_ptr()
+
+        def tape(t):
+            return N.ptr(tapes[t]) if tapes is not None else None
+
+        s = T - 1
+        N.check(L.dexmpm_g2p_grad(bp, 2 + s, N.ptr(sts[s]), N.ptr(sts[s + 1]), N.ptr(g_next), N.ptr(g), sp),
+                "dexmpm_g2p_grad")
+        for s in range(T - 1, -1, -1):
+            N.check(L.dexmpm_grid_op_grad(bp, 2 + s, N.ptr(poses[s]), N.ptr(poses[s + 1]), N.ptr(bgrad[s]),
+                                          N.ptr(bgrad[s + 1]), sp), "dexmpm_grid_op_grad")
+            if s > 0:
+                # gradients: of state s + 1 in g_next, of state s in g; the x
+                # gradient of state s - 1 goes to g_next
+                N.check(L.dexmpm_p2g_g2p_grad(bp, 2 + s, 1 + s, N.ptr(sts[s]), N.ptr(sts[s - 1]), N.ptr(g_next),
+                                              N.ptr(g), N.ptr(g_next), tape(s), sp), "dexmpm_p2g_g2p_grad")
+            else:
+                N.check(L.dexmpm_p2g_grad(bp, 2, N.ptr(sts[0]), N.ptr(g_next), N.ptr(g), tape(0), sp),
+                        "dexmpm_p2g_grad")
+            g_next, g = g, g_next
+        self.launches += 2 * T + 1
+        return g_next
+
     def clear_slots(self, first: int, last: int):
         """Make grid slots [first, last) clean (their adjoint will not run)."""
         N.check(self.lib.dexmpm_clear_slots(self._bp, int(first), int(last), N.stream_ptr()), "dexmpm_clear_slots")
@@ -432,13 +467,20 @@ class Rollout:
                 t = k * T + s
                 E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1])
                 src = self.ring[s + 1]
+        if self.keep_grids:
+            sts = [self.ckpt[k]] + [self.ring[s] for s in range(1, T)] + [self.ckpt[k + 1]]
+            out = E.run_adjoint(sts, self.gbuf[1], self.gbuf[0], self.poses[k * T:k * T + T + 1],
+                                self.bgrad[k * T:k * T + T + 1], tapes=self.tape)
+            if out is not self.gbuf[1]:
+                self.gbuf[1].copy_(out)
+            return
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):
             t = k * T + s
             cur = self.ckpt[k] if s == 0 else self.ring[s]
             nxt = self.ckpt[k + 1] if s == T - 1 else self.ring[s + 1]
             E.substep_grad(cur, nxt, g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
-                           self.bgrad[t + 1], slot=(2 + s) if self.keep_grids else None, tape=self._tape(s))
+                           self.bgrad[t + 1], tape=self._tape(s))
             g_next, g = g, g_next
         if T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])

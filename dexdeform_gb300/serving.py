@@ -100,13 +100,10 @@ class _Batch:
     def _backward(self):
         E = self.E
         E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
-        g_next, g = self.gbuf[1], self.gbuf[0]
-        for s in range(self.T - 1, -1, -1):
-            E.substep_grad(self.slot[s], self.slot[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s, tape=self.tape[s])
-            g_next, g = g, g_next
-        if self.T % 2 == 1:
-            self.gbuf[1].copy_(self.gbuf[0])
+        out = E.run_adjoint([self.slot[s] for s in range(self.T + 1)], self.gbuf[1], self.gbuf[0], self.poses,
+                            self.bgrad, tapes=self.tape)
+        if out is not self.gbuf[1]:
+            self.gbuf[1].copy_(out)
 
     def run(self, kind: str):
         run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward, self.use_graphs)

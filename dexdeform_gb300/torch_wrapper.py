@@ -58,13 +58,10 @@ class DiffSim:
     def _bwd(self):
         E = self.E
         E.run_substeps([self.ring[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
-        g_next, g = self.gbuf[1], self.gbuf[0]
-        for s in range(self.T - 1, -1, -1):
-            E.substep_grad(self.ring[s], self.ring[s + 1], g_next, g, self.poses[s], self.poses[s + 1],
-                           self.bgrad[s], self.bgrad[s + 1], slot=2 + s, tape=self.tape[s])
-            g_next, g = g, g_next
-        if self.T % 2 == 1:
-            self.gbuf[1].copy_(self.gbuf[0])
+        out = E.run_adjoint([self.ring[s] for s in range(self.T + 1)], self.gbuf[1], self.gbuf[0], self.poses,
+                            self.bgrad, tapes=self.tape)
+        if out is not self.gbuf[1]:
+            self.gbuf[1].copy_(out)
 
     def forward(self, state: torch.Tensor, poses: torch.Tensor) -> torch.Tensor:
         self.ring[0].copy_(state)

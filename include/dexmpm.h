@@ -265,6 +265,17 @@ int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const fl
 int dexmpm_p2g_grad(const DexBatch *b, int slot, const float *s, const float *g_next, float *g, const float *tape,
                     dexmpm_stream_t stream);
 
+/* P2G adjoint of substep t (grid slot `slot`, after its grid-update adjoint)
+ * fused with the G2P adjoint of substep t - 1 (grid slot prev_slot): s is
+ * state t, prev_s state t - 1, g_next the gradient of state t + 1 (its F is
+ * read), g the gradient of state t (its x holds the G2P adjoint's part; its F
+ * is written), g_prev the gradient of state t - 1 (its x is written; may be
+ * g_next).  The x, v, C gradients of state t pass between the two adjoints in
+ * registers and are not stored.  Same results as dexmpm_p2g_grad(slot) +
+ * dexmpm_g2p_grad(prev_slot) apart from those three stores, in one launch. */
+int dexmpm_p2g_g2p_grad(const DexBatch *b, int slot, int prev_slot, const float *s, const float *prev_s,
+                        const float *g_next, float *g, float *g_prev, const float *tape, dexmpm_stream_t stream);
+
 /* Clear grid slots [first, last) whose adjoint will not run (their listed
  * blocks, flags and list counts), e.g. substeps kept for an adjoint that was
  * not taken.  No counterpart in the reference. */

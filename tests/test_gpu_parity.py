@@ -417,3 +417,45 @@ def test_fused_substeps_equal_unfused(cuda):
     # float-atomic ordering only: ~1e-5 after 10 substeps from this state
     for other in finals[1:]:
         assert rel(other.cpu().numpy(), finals[0].cpu().numpy()) < 1e-4
+
+
+def test_fused_adjoint_equals_unfused(cuda):
+    """BatchEngine.run_adjoint (each P2G adjoint fused with the previous
+    substep's G2P adjoint, the x, v, C gradients passed in registers) against
+    the same T adjoint substeps launched one kernel at a time, after the same
+    kept forward with a tape."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec
+    envs = W.batch_envs(7, n_envs=3, steps=10, n_lo=500, n_hi=3000)
+    T = 10
+    outs = []
+    for mode in ("unfused", "fused"):
+        E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=T + 2)
+        poses = torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
+                             device="cuda")
+        sts = E.new_slots(T + 1)
+        sts[0].copy_(E.pack_state([W.perturb_state(e, seed=3, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+                                   for e in envs]))
+        tapes = E.new_tape(T)
+        E.run_substeps([sts[t] for t in range(T + 1)], poses, kept=True, tapes=tapes)
+        gen = torch.Generator(device="cuda").manual_seed(11)
+        g_next = torch.randn(sts[T].shape, device="cuda", generator=gen)
+        g = torch.empty_like(g_next)
+        nb = max(E.n_bodies, 1)
+        bg = torch.zeros((T + 1, nb, 8), device="cuda")
+        if mode == "unfused":
+            for s in range(T - 1, -1, -1):
+                E.substep_grad(sts[s], sts[s + 1], g_next, g, poses[s], poses[s + 1], bg[s], bg[s + 1], slot=2 + s,
+                               tape=tapes[s])
+                g_next, g = g, g_next
+            out = g_next
+        else:
+            out = E.run_adjoint([sts[t] for t in range(T + 1)], g_next, g, poses, bg, tapes=tapes)
+        assert E.error_word() == 0
+        assert int(E.block_count[2:].sum()) == 0  # the adjoint cleared every kept slot
+        outs.append((sts[T].clone(), out.clone(), bg.clone()))
+    # float-atomic ordering only (see the kept-env-step test for the levels)
+    (sa, ga, ba), (sb, gb, bb) = outs
+    assert rel(sa.cpu().numpy(), sb.cpu().numpy()) < 2e-4
+    assert rel(ga.cpu().numpy(), gb.cpu().numpy()) < 5e-4
+    assert rel(ba.cpu().numpy(), bb.cpu().numpy()) < 5e-4
