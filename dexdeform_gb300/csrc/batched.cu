@@ -33,14 +33,25 @@ using namespace dexmpm;
 
 // Compile-time tuning knobs.  Defaults were picked by timing every kernel on
 // GB300 over the 64-env batch: minimum resident CTAs per SM (register caps:
-// P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint 128) and the unrolling
-// of the outer loop over the 27 stencil nodes in the adjoints (full unrolling
-// keeps the weight arrays out of local memory).
+// P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint and the fused adjoint
+// 128, grid update and its adjoint 64 -- four 256-thread CTAs per SM, so that
+// the persistent grid kernels cover the active blocks in fewer rounds) and
+// the unrolling of the outer loop over the 27 stencil nodes in the adjoints
+// (full unrolling keeps the weight arrays out of local memory).
 #ifndef DEX_P2G_MINB
 #define DEX_P2G_MINB 3
 #endif
 #ifndef DEX_P2G_GRAD_MINB
 #define DEX_P2G_GRAD_MINB 4
+#endif
+#ifndef DEX_P2G2G_GRAD_MINB
+#define DEX_P2G2G_GRAD_MINB 4
+#endif
+#ifndef DEX_GRID_OP_MINB
+#define DEX_GRID_OP_MINB 4
+#endif
+#ifndef DEX_GRID_OP_GRAD_MINB
+#define DEX_GRID_OP_GRAD_MINB 4
 #endif
 #ifndef DEX_G2P2G_MINB
 #define DEX_G2P2G_MINB 3
@@ -560,7 +571,7 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
 // integrator.cu:647-777 on the active blocks of slot X, then (Y >= 0) clearing
 // of the blocks slot Y used.  The last CTA to finish resets the list count of
 // Y (ticket on done_counter; no CTA waits on another).
-__global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, int Y, const float *__restrict__ pose,
+__global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, int X, int Y, const float *__restrict__ pose,
                                                  const float *__restrict__ next_pose) {
   const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
   const int per_cta = blockDim.x >> 6;
@@ -568,34 +579,42 @@ __global__ void __launch_bounds__(256) k_grid_op(DexBatch B, int X, int Y, const
   const float4 *__restrict__ grid = reinterpret_cast<const float4 *>(slot_grid(B, X));
   float4 *vout = reinterpret_cast<float4 *>(slot_vout(B, X));
   const int32_t *list = slot_list(B, X);
-  for (int item = blockIdx.x * per_cta + sub; item < cnt; item += gridDim.x * per_cta) {
-    const int blk = list[item];
-    const DexEnv E = B.envs[B.block_env[blk]];
+  // node velocity of this cell of block (bx, by, bz) of env E
+  auto update = [&](const DexEnv &E, int bx, int by, int bz, float4 g, uint32_t near) -> float4 {
+    if (!(g.w > kMassEps)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
+    const float inv_m = 1.f / g.w;
+    f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
+    const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
+    for (uint32_t rest = near; rest; rest &= rest - 1u) {
+      const int b = __ffs(rest) - 1;
+      BodyPose cur, nxt;
+      BodyShape sh;
+      load_pose(pose, E.body_off + b, cur);
+      load_pose(next_pose, E.body_off + b, nxt);
+      load_shape(B.body_shape, E.body_off + b, sh);
+      contact_forward(gx, v, cur, nxt, sh, E.dt);
+    }
+    v = boundary_forward(v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
+    return make_float4(v.x, v.y, v.z, g.w);
+  };
+  auto coords = [](const DexEnv &E, int blk, int &bx, int &by, int &bz) {
     const int local = blk - E.blk_off;
     const int nby = E.gy >> 2, nbz = E.gz >> 2;
-    const int bx = local / (nby * nbz), by = (local / nbz) % nby, bz = local % nbz;
-    const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
+    bx = local / (nby * nbz);
+    by = (local / nbz) % nby;
+    bz = local % nbz;
+  };
+  const int stride = gridDim.x * per_cta;
+  for (int item = blockIdx.x * per_cta + sub; item < cnt; item += stride) {
+    const int blk = list[item];
+    const DexEnv E = B.envs[B.block_env[blk]];
+    int bx, by, bz;
+    coords(E, blk, bx, by, bz);
     const int ci = (blk << 6) + cell;
     const float4 g = grid[ci];
     const uint32_t near = bodies_near_block(B, E, pose, bx, by, bz, E.n_bodies);
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (g.w > kMassEps) {
-      const float inv_m = 1.f / g.w;
-      f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
-      const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
-      for (uint32_t rest = near; rest; rest &= rest - 1u) {
-        const int b = __ffs(rest) - 1;
-        BodyPose cur, nxt;
-        BodyShape sh;
-        load_pose(pose, E.body_off + b, cur);
-        load_pose(next_pose, E.body_off + b, nxt);
-        load_shape(B.body_shape, E.body_off + b, sh);
-        contact_forward(gx, v, cur, nxt, sh, E.dt);
-      }
-      v = boundary_forward(v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
-      out = make_float4(v.x, v.y, v.z, g.w);
-    }
-    vout[ci] = out;
+    vout[ci] = update(E, bx, by, bz, g, near);
   }
   if (Y < 0) return;
   // clear the blocks slot Y used
@@ -775,7 +794,7 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
 // dL/d(mv, m) written (zero where there is no mass), and dL/dv_out and the
 // slot's grid are zeroed after they are read, so the next use finds them
 // clean; the last CTA resets the slot's list.
-__global__ void __launch_bounds__(256, 3) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
+__global__ void __launch_bounds__(256, DEX_GRID_OP_GRAD_MINB) k_grid_op_grad(DexBatch B, int X, const float *__restrict__ pose,
                                                       const float *__restrict__ next_pose, float *__restrict__ bgrad,
                                                       float *__restrict__ next_bgrad) {
   const int sub = threadIdx.x >> 6, cell = threadIdx.x & 63;
@@ -1068,7 +1087,7 @@ __global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g_grad(DexBatch B,
 // read), G: gradients of state s (x read: the part from the G2P adjoint of
 // substep s; F written).  Gprev may be Gnext (different planes).
 template <bool kTape>
-__global__ void __launch_bounds__(128, DEX_P2G_GRAD_MINB) k_p2g2g_grad(DexBatch B, int X, int Xprev, const float *S,
+__global__ void __launch_bounds__(128, DEX_P2G2G_GRAD_MINB) k_p2g2g_grad(DexBatch B, int X, int Xprev, const float *S,
                                                     const float *Sprev, const float *Gnext, float *G, float *Gprev,
                                                     int split, const float *__restrict__ tape) {
   const int tile = blockIdx.x / split, part = blockIdx.x % split;
