@@ -198,7 +198,7 @@ def run_ours(args, rank, world, local):
         counts[E.p_off[e]:E.p_off[e] + env.n] = 1.0 / env.n
     g_final = torch.zeros_like(s0)
     from dexdeform_gb300.autotune import tune
-    tuned = tune(E, s0, R.poses[:2], use_cache=False)
+    tuned = tune(E, s0, R.poses[:4], use_cache=False)
 
     def loss_grad(final):
         # L = sum_e mean_p |x - target|^2 ; dL/dx = 2 (x - target) / n_e

@@ -2,8 +2,9 @@
 
 Picks the particle tile size (CTA size of the particle kernels) and the number
 of persistent CTAs of the grid kernels for a given batch by timing a few
-forward (and, for gradient engines, adjoint) substeps of each candidate on the
-batch itself, with CUDA events on the launching stream.  Results are cached in
+forward substeps (and, for gradient engines, their adjoint) of each candidate
+on the batch itself, launched as a rollout launches them, with CUDA events on
+the launching stream.  Results are cached in
 memory and in a JSON file keyed by (grid size, particle-count bucket, number
 of envs bucket, gradient or not), so a shape is tuned once per process or
 machine.
@@ -59,23 +60,30 @@ def tune(E: BatchEngine, state: torch.Tensor, poses: torch.Tensor, reps: int = 3
         if key in _CACHE:
             E.retune(*_CACHE[key])
             return _CACHE[key]
-    scratch = E.new_slots(2)
+    # a short rollout piece as the Rollout runs it: T substeps with each G2P
+    # fused with the next P2G, and (gradient engines with kept grid slots)
+    # their adjoint with each P2G adjoint fused with the previous G2P adjoint
+    T = 3
+    scratch = list(E.new_slots(T))
+    sts = [state] + scratch
+    pz = torch.stack([poses[min(i, poses.shape[0] - 1)] for i in range(T + 1)])
+    kept = E.grad and E.n_grid_slots >= T + 2
+    tapes = E.new_tape(T) if kept else None
     g_slots = E.new_slots(2) if E.grad else None
-    bg = torch.zeros((2,) + tuple(poses.shape[1:]), device=E.device)
-    # gradient engines with kept grid slots run the adjoint on the slot the
-    # forward filled, as a rollout does
-    kept = 2 if (E.grad and E.n_grid_slots > 2) else None
+    bg = torch.zeros((T + 1,) + tuple(poses.shape[1:]), device=E.device)
     best, best_t = None, math.inf
     for tile, ctas in candidates:
         E.retune(tile, ctas)
 
         def run():
-            if E.grad:
-                E.substep(state, scratch[0], poses[0], poses[1], slot=kept)
-                E.substep_grad(state, scratch[0], g_slots[0], g_slots[1], poses[0], poses[1], bg[0], bg[1],
-                               slot=kept)
-            else:
+            if kept:
+                E.run_substeps(sts, pz, kept=True, tapes=tapes)
+                E.run_adjoint(sts, g_slots[0], g_slots[1], pz, bg, tapes=tapes)
+            elif E.grad:
                 E.substep(state, scratch[0], poses[0], poses[1])
+                E.substep_grad(state, scratch[0], g_slots[0], g_slots[1], poses[0], poses[1], bg[0], bg[1])
+            else:
+                E.run_substeps(sts, pz)
 
         run()
         torch.cuda.synchronize()

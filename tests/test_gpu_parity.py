@@ -459,3 +459,23 @@ def test_fused_adjoint_equals_unfused(cuda):
     assert rel(sa.cpu().numpy(), sb.cpu().numpy()) < 2e-4
     assert rel(ga.cpu().numpy(), gb.cpu().numpy()) < 5e-4
     assert rel(ba.cpu().numpy(), bb.cpu().numpy()) < 5e-4
+
+
+def test_autotuner_picks_a_candidate_and_leaves_slots_clean(cuda):
+    """The launch-shape autotuner times each candidate on a short fused piece
+    of rollout (kept substeps and their fused adjoint), applies the fastest,
+    and leaves the engine usable: no error, every kept slot cleared."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.autotune import tune
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec
+    envs = W.batch_envs(9, n_envs=3, steps=4, n_lo=500, n_hi=2000)
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=8)
+    poses = torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
+                         device="cuda")
+    s0 = E.new_slots(1)[0]
+    s0.copy_(E.pack_state([e.state() for e in envs]))
+    cands = [(64, 304), (128, 608)]
+    best = tune(E, s0, poses, reps=1, use_cache=False, candidates=cands)
+    assert best in cands and (E.tile_size, E.grid_ctas) == best
+    assert E.error_word() == 0
+    assert int(E.block_count[2:].sum()) == 0
