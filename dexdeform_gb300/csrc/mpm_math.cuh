@@ -674,23 +674,37 @@ DX_HD void contact_backward(f3 gx, f3 vo, f3 &gv, const BodyPose &cur, const Bod
 // integrator.cu:102-108
 DX_HD float clamp_gap(float a) { return a >= 0.f ? fmaxf(a, 1e-6f) : fminf(a, -1e-6f); }
 
-// Gradient of F_tmp from gradients of (U, sigma, V) (integrator.cu:131-159).
-// sigma_j^2 - sigma_i^2 is formed as (d_j - d_i)(sigma_j + sigma_i).
+// Gradient of F_tmp from gradients of (U, sigma, V) (integrator.cu:131-159):
+//   gF = gF_direct + U [ (F o (U^T gU - gU^T U)) S + S (F o (V^T gV - gV^T V)) + diag(gs) ] V^T
+// with F_ij = 1 / clamp_gap(sigma_j^2 - sigma_i^2) off the diagonal, S = diag(sigma).
+// sigma_j^2 - sigma_i^2 is formed as (d_j - d_i)(sigma_j + sigma_i), which is
+// exactly antisymmetric in (i, j), so F_ji = -F_ij except at a zero gap, where
+// clamp_gap gives +1e-6 for both orders; U^T gU - gU^T U is antisymmetric.  One
+// reciprocal and two 3-term differences per pair, then U M V^T.
 DX_HD m33 svd_backward(const SVD3 &sv, const m33 &gU, f3 gs, const m33 &gV, const m33 &gFtmp_direct) {
-  float d[3] = {sv.d.x, sv.d.y, sv.d.z}, s[3] = {sv.s.x, sv.s.y, sv.s.z};
-  m33 FF;
+  const float d[3] = {sv.d.x, sv.d.y, sv.d.z}, s[3] = {sv.s.x, sv.s.y, sv.s.z};
+  m33 M = mzero();
+  M.a[0][0] = gs.x;
+  M.a[1][1] = gs.y;
+  M.a[2][2] = gs.z;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) FF.a[i][j] = (i == j) ? 0.f : 1.f / clamp_gap((d[j] - d[i]) * (s[j] + s[i]));
-  m33 Sg = mdiag(sv.s);
-  m33 Ut = mT(sv.U), Vt = mT(sv.V);
-  m33 sig_term = usv(sv.U, gs, sv.V);
-  m33 u_in = hadamard(FF, mm(Ut, gU) - mm(mT(gU), sv.U));
-  m33 v_in = hadamard(FF, mm(Vt, gV) - mm(mT(gV), sv.V));
-  m33 u_term = mm(mm(sv.U, mm(u_in, Sg)), Vt);
-  m33 v_term = mm(sv.U, mm(Sg, mm(v_in, Vt)));
-  return gFtmp_direct + u_term + sig_term + v_term;
+    for (int j = i + 1; j < 3; ++j) {
+      const float gap = (d[j] - d[i]) * (s[j] + s[i]);
+      const float fij = 1.f / clamp_gap(gap);
+      const float fji = gap == 0.f ? fij : -fij;
+      float wu = 0.f, wv = 0.f;  // (U^T gU - gU^T U)_ij, (V^T gV - gV^T V)_ij
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        wu += sv.U.a[k][i] * gU.a[k][j] - gU.a[k][i] * sv.U.a[k][j];
+        wv += sv.V.a[k][i] * gV.a[k][j] - gV.a[k][i] * sv.V.a[k][j];
+      }
+      // entries (i, j) and (j, i) of u_in S + S v_in (u_in = F o (..), v_in likewise)
+      M.a[i][j] = fij * wu * s[j] + s[i] * fij * wv;
+      M.a[j][i] = -fji * wu * s[i] - s[j] * fji * wv;
+    }
+  return gFtmp_direct + mm(mm(sv.U, M), mT(sv.V));
 }
 
 }  // namespace dexmpm

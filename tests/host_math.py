@@ -51,6 +51,16 @@ def constitutive(F, C, dt, mly):
     return nF, P, J
 
 
+def svd_backward(U, sig, d, V, gU, gs, gV, gdirect):
+    """The product's SVD adjoint (mpm_math.cuh svd_backward) on the host."""
+    L = load()
+    U, sig, d, V, gU, gs, gV, gdirect = (f32(a) for a in (U, sig, d, V, gU, gs, gV, gdirect))
+    out = np.zeros_like(gdirect)
+    L.host_svd_backward(ctypes.c_int(U.shape[0]), _p(U), _p(sig), _p(d), _p(V), _p(gU), _p(gs), _p(gV), _p(gdirect),
+                        _p(out))
+    return out
+
+
 def substep(env, st, t):
     """One forward substep of workloads.Env `env` from state dict st at substep t."""
     L = load()

@@ -33,6 +33,19 @@ void host_constitutive(int n, const float *F, const float *C, float dt, const fl
     J[p] = o.J;
   }
 }
+// gradient of F_tmp from gradients of (U, sigma, V) for given SVDs (U, sig, d, V)
+void host_svd_backward(int n, const float *U, const float *sig, const float *d, const float *V, const float *gU,
+                       const float *gs, const float *gV, const float *gdirect, float *out) {
+  for (int p = 0; p < n; ++p) {
+    SVD3 sv;
+    sv.U = load9(U + 9 * p);
+    sv.V = load9(V + 9 * p);
+    sv.s = mk3(sig[3 * p], sig[3 * p + 1], sig[3 * p + 2]);
+    sv.d = mk3(d[3 * p], d[3 * p + 1], d[3 * p + 2]);
+    store9(out + 9 * p, svd_backward(sv, load9(gU + 9 * p), mk3(gs[3 * p], gs[3 * p + 1], gs[3 * p + 2]),
+                                     load9(gV + 9 * p), load9(gdirect + 9 * p)));
+  }
+}
 }
 
 // Serial host emulation of one forward substep with the product's FP32

@@ -89,6 +89,54 @@ def test_product_stress_is_cancellation_free(oracle_mod):
     assert rel(J, Jd) < 1e-7
 
 
+def test_svd_adjoint_matches_expanded_formula():
+    """The product's compact SVD adjoint (one reciprocal per singular-value
+    pair, U M V^T) against the reference's expanded form in FP64
+    (integrator.cu:131-159): F = 1/clamp_gap(sigma_j^2 - sigma_i^2) off the
+    diagonal, u = F o (U^T gU - gU^T U), v = F o (V^T gV - gV^T V),
+    gF = gF_direct + U u S V^T + U diag(gs) V^T + U S v V^T, including
+    equal singular values (zero gaps, where clamp_gap gives +1e-6 for both
+    orders) and tiny gaps."""
+    import host_math as H
+    rng = np.random.default_rng(4)
+    n = 600
+
+    def rot(k):
+        q = rng.normal(size=(k, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        w, x, y, z = q.T
+        return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+                         np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+                         np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+    U, V = rot(n).astype(np.float32), rot(n).astype(np.float32)
+    d = (rng.normal(size=(n, 3)) * 0.05).astype(np.float32)
+    d[:100] = 0.0                                  # at rest: all gaps zero
+    d[100:200, 1] = d[100:200, 0]                  # one repeated singular value
+    d[200:300, 2] = d[200:300, 1] + 1e-7           # a tiny gap
+    sig = (1.0 + d.astype(np.float64)).astype(np.float32)
+    gU, gV, gd = (rng.normal(size=(n, 3, 3)).astype(np.float32) for _ in range(3))
+    gs = rng.normal(size=(n, 3)).astype(np.float32)
+    out = H.svd_backward(U, sig, d, V, gU, gs, gV, gd)
+
+    def clamp_gap(a):
+        return np.where(a >= 0, np.maximum(a, 1e-6), np.minimum(a, -1e-6))
+
+    Ud, Vd, dd, sd = (a.astype(np.float64) for a in (U, V, d, sig))
+    gap = (dd[:, None, :] - dd[:, :, None]) * (sd[:, None, :] + sd[:, :, None])  # [n, i, j]: (d_j - d_i)(s_j + s_i)
+    F = np.where(np.eye(3, dtype=bool)[None], 0.0, 1.0 / clamp_gap(gap))
+    UtgU = np.einsum("nki,nkj->nij", Ud, gU)
+    VtgV = np.einsum("nki,nkj->nij", Vd, gV)
+    u_in = F * (UtgU - np.swapaxes(UtgU, 1, 2))
+    v_in = F * (VtgV - np.swapaxes(VtgV, 1, 2))
+    S = np.einsum("ni,ij->nij", sd, np.eye(3))
+    G = np.einsum("nij,njk->nik", u_in, S) + np.einsum("nij,njk->nik", S, v_in) + \
+        np.einsum("ni,ij->nij", gs.astype(np.float64), np.eye(3))
+    ref = gd + np.einsum("nij,njk,nlk->nil", Ud, G, Vd)
+    for sl in (slice(0, 100), slice(100, 200), slice(200, 300), slice(300, n)):
+        assert rel(out[sl], ref[sl]) < 2e-6, sl
+
+
 def test_host_substep_matches_oracle_off_rest(oracle_mod):
     """The product arithmetic (host build) for one substep from a non-rest
     state meets the 1e-5 bar against the FP64 oracle."""
