@@ -989,40 +989,8 @@ __device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEn
   const f3 g_v = gw * m;
   if constexpr (kTape) forward_state();
 
-  // stress -> (U, V, sigma, F_tmp) gradients (integrator.cu:541-625)
-  const m33 &nF = pl.newF;
-  const m33 NmR = usv(sv.U, pl.dm1, sv.V);  // newF - U V^T without cancellation
-  const m33 g_r = mm(g_stress, nF) * (-2.f * mu);
-  m33 gU = mm(g_r, sv.V);
-  m33 gV = mm(mT(g_r), sv.U);
-  const m33 g_nF = ldm33(Gnext, N, PF, p) + (mm(mT(g_stress), NmR) + mm(g_stress, nF)) * (2.f * mu);
-  const float g_J = ((2.f * pl.J - 1.f) * lam) * trace(g_stress);
-  f3 g_s = mk3(0.f, 0.f, 0.f);
-  m33 g_Ft = mzero();
-  if (pl.yielded) {
-    const f3 ee = pl.expe;
-    const m33 ed = mdiag(ee);
-    gU += mm(mm(g_nF, sv.V), ed);
-    gV += mm(mm(mT(g_nF), sv.U), ed);
-    const m33 t = mm(mm(mT(sv.U), g_nF), sv.V);
-    const f3 Fpart = mk3(t.a[0][0], t.a[1][1], t.a[2][2]);
-    const f3 Jpart = mk3(g_J * ee.y * ee.z, g_J * ee.x * ee.z, g_J * ee.x * ee.y);
-    f3 g_e = hadamard(ee, Jpart + Fpart);
-    const f3 eh = pl.eps_hat;
-    const float ehn = pl.eps_hat_norm;
-    f3 g_eh = g_e * (-pl.delta_gamma / ehn);
-    const float g_ehn = -dot(eh * (1.f / ehn), g_e) * (ys / (2.f * mu)) / ehn;
-    g_eh += eh * (g_ehn / ehn);
-    const float sm = (g_eh.x + g_eh.y + g_eh.z) * (1.f / 3.f);
-    g_e += mk3(g_eh.x - sm, g_eh.y - sm, g_eh.z - sm);
-    if (sv.s.x >= kSigClip) g_s.x += g_e.x / sv.s.x;
-    if (sv.s.y >= kSigClip) g_s.y += g_e.y / sv.s.y;
-    if (sv.s.z >= kSigClip) g_s.z += g_e.z / sv.s.z;
-  } else {
-    g_s = mk3(g_J * sv.s.y * sv.s.z, g_J * sv.s.x * sv.s.z, g_J * sv.s.x * sv.s.y);
-    g_Ft = g_nF;
-  }
-  const m33 Gt = svd_backward(sv, gU, g_s, gV, g_Ft);
+  // stress and projection -> F_tmp gradient (integrator.cu:541-625)
+  const m33 Gt = plastic_stress_backward(sv, pl, g_stress, ldm33(Gnext, N, PF, p), mu, lam, ys);
   // F_tmp = (I + dt C) F
   const m33 gC_total = g_C + mm(Gt, mT(F)) * E.dt;
   m33 IdtC = C * E.dt;

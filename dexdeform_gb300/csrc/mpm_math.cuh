@@ -707,4 +707,98 @@ DX_HD m33 svd_backward(const SVD3 &sv, const m33 &gU, f3 gs, const m33 &gV, cons
   return gFtmp_direct + mm(mm(sv.U, M), mT(sv.V));
 }
 
+// The same adjoint for callers that hold the rotated gradients: ku_p and kv_p
+// are entry (i, j) of U^T gU - gU^T U and V^T gV - gV^T V for the pairs
+// p = (0,1), (0,2), (1,2); returns U (M + madd) V^T (without a direct term).
+// With opposite (kv = -ku, `opposite`) the pair entries F_ij ku (s_j - s_i)
+// are formed from d_j - d_i, without the cancellation of the two products.
+DX_HD m33 svd_backward_rot(const SVD3 &sv, const float ku[3], const float kv[3], f3 gs, const m33 &madd,
+                           bool opposite) {
+  const float d[3] = {sv.d.x, sv.d.y, sv.d.z}, s[3] = {sv.s.x, sv.s.y, sv.s.z};
+  m33 M = madd;
+  M.a[0][0] += gs.x;
+  M.a[1][1] += gs.y;
+  M.a[2][2] += gs.z;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int i = q == 2 ? 1 : 0, j = q == 0 ? 1 : 2;
+    const float gap = (d[j] - d[i]) * (s[j] + s[i]);
+    const float fij = 1.f / clamp_gap(gap);
+    const float fji = gap == 0.f ? fij : -fij;
+    if (opposite) {
+      const float k = ku[q] * (d[j] - d[i]);
+      M.a[i][j] += fij * k;
+      M.a[j][i] += fji * k;
+    } else {
+      M.a[i][j] += fij * ku[q] * s[j] + s[i] * fij * kv[q];
+      M.a[j][i] -= fji * ku[q] * s[i] + s[j] * fji * kv[q];
+    }
+  }
+  return mm(mm(sv.U, M), mT(sv.V));
+}
+
+// Adjoint of the return mapping and stress (integrator.cu:541-625): dL/dF_tmp
+// from dL/dP (g_stress, P = 2 mu (newF - R) newF^T + lam J (J - 1) I as
+// `constitutive` returns it) and the incoming dL/dnewF (GF), given the SVD of
+// F_tmp and the constitutive intermediates.  Worked in the frame of the SVD:
+// with newF = U D V^T (D the projected singular values, sigma when not
+// yielded), R = U V^T and X = U^T g_stress U,
+//   U^T dL/dR V = -2 mu X D =: W,
+//   U^T dL/dnewF V = U^T GF V + 2 mu (X^T (D - 1) + X D) = U^T GF V + Q,
+// and the SVD adjoint needs only the antisymmetric parts of U^T dL/dU and
+// V^T dL/dV: W - W^T and W^T - W, plus T E - (T E)^T and T^T E - (T^T E)^T
+// after a yield (T = U^T dL/dnewF V, E = diag(D)).  Not yielded, newF is F_tmp
+// itself and dL/dnewF passes to dL/dF_tmp directly.
+DX_HD m33 plastic_stress_backward(const SVD3 &sv, const Plastic &pl, const m33 &g_stress, const m33 &GF, float mu,
+                                  float lam, float ys) {
+  const m33 X = mm(mT(sv.U), mm(g_stress, sv.U));
+  const f3 D3 = pl.expe, Dm3 = pl.dm1;
+  const float Dv[3] = {D3.x, D3.y, D3.z}, Dm[3] = {Dm3.x, Dm3.y, Dm3.z};
+  m33 Q;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Q.a[i][j] = (X.a[j][i] * Dm[j] + X.a[i][j] * Dv[j]) * (2.f * mu);
+  const float g_J = ((2.f * pl.J - 1.f) * lam) * trace(g_stress);
+  float ku[3], kv[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int i = q == 2 ? 1 : 0, j = q == 0 ? 1 : 2;
+    const float w = (-2.f * mu) * (X.a[i][j] * Dv[j] - X.a[j][i] * Dv[i]);  // W_ij - W_ji
+    ku[q] = w;
+    kv[q] = -w;
+  }
+  f3 g_s;
+  if (pl.yielded) {
+    const m33 T = mm(mT(sv.U), mm(GF, sv.V)) + Q;
+    const f3 ee = pl.expe;
+    const float ev[3] = {ee.x, ee.y, ee.z};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int i = q == 2 ? 1 : 0, j = q == 0 ? 1 : 2;
+      ku[q] += T.a[i][j] * ev[j] - T.a[j][i] * ev[i];
+      kv[q] += T.a[j][i] * ev[j] - T.a[i][j] * ev[i];
+    }
+    const f3 Fpart = mk3(T.a[0][0], T.a[1][1], T.a[2][2]);
+    const f3 Jpart = mk3(g_J * ee.y * ee.z, g_J * ee.x * ee.z, g_J * ee.x * ee.y);
+    f3 g_e = hadamard(ee, Jpart + Fpart);
+    const f3 eh = pl.eps_hat;
+    const float ehn = pl.eps_hat_norm;
+    f3 g_eh = g_e * (-pl.delta_gamma / ehn);
+    const float g_ehn = -dot(eh * (1.f / ehn), g_e) * (ys / (2.f * mu)) / ehn;
+    g_eh += eh * (g_ehn / ehn);
+    const float sm = (g_eh.x + g_eh.y + g_eh.z) * (1.f / 3.f);
+    g_e += mk3(g_eh.x - sm, g_eh.y - sm, g_eh.z - sm);
+    g_s = mk3(0.f, 0.f, 0.f);
+    if (sv.s.x >= kSigClip) g_s.x += g_e.x / sv.s.x;
+    if (sv.s.y >= kSigClip) g_s.y += g_e.y / sv.s.y;
+    if (sv.s.z >= kSigClip) g_s.z += g_e.z / sv.s.z;
+    return svd_backward_rot(sv, ku, kv, g_s, mzero(), false);
+  } else {
+    // dL/dF_tmp receives dL/dnewF directly: GF + U Q V^T
+    g_s = mk3(g_J * sv.s.y * sv.s.z, g_J * sv.s.x * sv.s.z, g_J * sv.s.x * sv.s.y);
+    return GF + svd_backward_rot(sv, ku, kv, g_s, Q, true);
+  }
+}
+
 }  // namespace dexmpm

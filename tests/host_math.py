@@ -61,6 +61,19 @@ def svd_backward(U, sig, d, V, gU, gs, gV, gdirect):
     return out
 
 
+def stress_backward(F, C, dt, mly, gP, gF):
+    """dL/dF_tmp of the product's return mapping and stress (mpm_math.cuh
+    plastic_stress_backward); returns it with F_tmp and the yield flags."""
+    L = load()
+    F, C, mly, gP, gF = (f32(a) for a in (F, C, mly, gP, gF))
+    n = F.shape[0]
+    out, Ft = np.zeros_like(F), np.zeros_like(F)
+    y = np.zeros(n, np.int32)
+    L.host_stress_backward(ctypes.c_int(n), _p(F), _p(C), ctypes.c_float(dt), _p(mly), _p(gP), _p(gF), _p(out),
+                           _p(Ft), y.ctypes.data_as(ctypes.c_void_p))
+    return out, Ft, y.astype(bool)
+
+
 def substep(env, st, t):
     """One forward substep of workloads.Env `env` from state dict st at substep t."""
     L = load()

@@ -33,6 +33,22 @@ void host_constitutive(int n, const float *F, const float *C, float dt, const fl
     J[p] = o.J;
   }
 }
+// dL/dF_tmp of the return mapping and stress from dL/dP (gP) and dL/dnewF (gF),
+// with the product's SVD and constitutive intermediates of F_tmp = (I + dt C) F;
+// also returns F_tmp and the yield flag
+void host_stress_backward(int n, const float *F, const float *C, float dt, const float *mly, const float *gP,
+                          const float *gF, float *out, float *Ftmp, int *yielded) {
+  for (int p = 0; p < n; ++p) {
+    m33 E = deviation_tmp(load9(F + 9 * p), load9(C + 9 * p), dt);
+    SVD3 s = svd3_from_deviation(E);
+    m33 Ft = E; Ft.a[0][0] += 1.f; Ft.a[1][1] += 1.f; Ft.a[2][2] += 1.f;
+    Plastic o = constitutive(s, Ft, mly[3 * p], mly[3 * p + 1], mly[3 * p + 2]);
+    store9(out + 9 * p, plastic_stress_backward(s, o, load9(gP + 9 * p), load9(gF + 9 * p), mly[3 * p],
+                                                mly[3 * p + 1], mly[3 * p + 2]));
+    store9(Ftmp + 9 * p, Ft);
+    yielded[p] = o.yielded ? 1 : 0;
+  }
+}
 // gradient of F_tmp from gradients of (U, sigma, V) for given SVDs (U, sig, d, V)
 void host_svd_backward(int n, const float *U, const float *sig, const float *d, const float *V, const float *gU,
                        const float *gs, const float *gV, const float *gdirect, float *out) {

@@ -137,6 +137,59 @@ def test_svd_adjoint_matches_expanded_formula():
         assert rel(out[sl], ref[sl]) < 2e-6, sl
 
 
+def _stress_objective(Ft, gP, gF, mu, lam, ys, sig_clip=0.05, norm_eps=1e-8):
+    """<gP, P(Ft)> + <gF, newF(Ft)> in FP64 for one F_tmp: the reference's von
+    Mises projection (integrator.cu:42-67) and fixed-corotated stress
+    2 mu (newF - R) newF^T + lam J (J - 1) I (integrator.cu:364-371)."""
+    U, s, Vt = np.linalg.svd(Ft)
+    e = np.log(np.where(s >= sig_clip, s, sig_clip))
+    eh = e - e.mean()
+    ehn = np.sqrt(eh @ eh + norm_eps)
+    dg = ehn - ys / (2 * mu)
+    nF = U @ np.diag(np.exp(e - dg * eh / ehn)) @ Vt if dg > 0 else Ft
+    R = U @ Vt
+    J = np.linalg.det(nF)
+    P = 2 * mu * (nF - R) @ nF.T + lam * J * (J - 1) * np.eye(3)
+    return float((gP * P).sum() + (gF * nF).sum())
+
+
+def test_stress_adjoint_matches_finite_differences():
+    """The product's adjoint of the return mapping and stress (worked in the
+    frame of the SVD) against central differences of the FP64 objective
+    <gP, P(F_tmp)> + <gF, newF(F_tmp)>, for states that do not yield and
+    states that yield, with well-separated singular values."""
+    import host_math as H
+    rng = np.random.default_rng(6)
+    n = 120
+    F = np.zeros((n, 3, 3), np.float32)
+    for k in range(n):
+        while True:
+            A = np.eye(3) + rng.normal(size=(3, 3)) * (0.02 if k < n // 2 else 0.15)
+            sv = np.linalg.svd(A, compute_uv=False)
+            if np.linalg.det(A) > 0.3 and np.min(np.abs(np.diff(sv))) > 2e-3:
+                break
+        F[k] = A
+    C = np.zeros_like(F)
+    mu, lam = 2083.33, 1388.89
+    ys = np.where(np.arange(n) < n // 2, 1e4, 20.0)      # first half cannot yield, second half yields
+    mly = np.stack([np.full(n, mu), np.full(n, lam), ys], 1).astype(np.float32)
+    gP = rng.normal(size=(n, 3, 3)).astype(np.float32)
+    gF = (rng.normal(size=(n, 3, 3)) * 1e3).astype(np.float32)
+    out, Ft, yielded = H.stress_backward(F, C, 0.0, mly, gP, gF)
+    assert not yielded[:n // 2].any() and yielded[n // 2:].mean() > 0.8
+    eps = 1e-6
+    for k in range(n):
+        Fk = Ft[k].astype(np.float64)
+        fd = np.zeros((3, 3))
+        for i in range(3):
+            for j in range(3):
+                dF = np.zeros((3, 3))
+                dF[i, j] = eps
+                fd[i, j] = (_stress_objective(Fk + dF, gP[k], gF[k], mu, lam, float(mly[k, 2]))
+                            - _stress_objective(Fk - dF, gP[k], gF[k], mu, lam, float(mly[k, 2]))) / (2 * eps)
+        assert rel(out[k], fd) < 2e-5, (k, bool(yielded[k]), rel(out[k], fd))
+
+
 def test_host_substep_matches_oracle_off_rest(oracle_mod):
     """The product arithmetic (host build) for one substep from a non-rest
     state meets the 1e-5 bar against the FP64 oracle."""
