@@ -56,9 +56,6 @@ using namespace dexmpm;
 #ifndef DEX_G2P2G_MINB
 #define DEX_G2P2G_MINB 3
 #endif
-#ifndef DEX_P2G_GRAD_UNROLL
-#define DEX_P2G_GRAD_UNROLL 3
-#endif
 #ifndef DEX_G2P_GRAD_UNROLL
 #define DEX_G2P_GRAD_UNROLL 3
 #endif
@@ -71,7 +68,6 @@ using namespace dexmpm;
 #define DEX_DIRECT_SEGS 8
 #endif
 constexpr int kG2pGradUnroll = DEX_G2P_GRAD_UNROLL;
-constexpr int kP2gGradUnroll = DEX_P2G_GRAD_UNROLL;
 
 namespace {
 
@@ -955,29 +951,67 @@ __device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEn
   const f3 a0c = mcol(A, 0) * E.dx, a1c = mcol(A, 1) * E.dx, a2c = mcol(A, 2) * E.dx;
   const f3 a0 = -(a0c * st.fx[0] + a1c * st.fx[1] + a2c * st.fx[2]);
   const f3 u = v * m;
-  // Gs = sum N gov ((i, j, k) - fx)^T dx = (sum N gov (i, j, k)^T - gw fx^T) dx
-  f3 g_x = mk3(0.f, 0.f, 0.f), gw = mk3(0.f, 0.f, 0.f);
-  f3 si = mk3(0.f, 0.f, 0.f), sj = mk3(0.f, 0.f, 0.f), sk = mk3(0.f, 0.f, 0.f);
-#pragma unroll kP2gGradUnroll
-  for (int i = 0; i < 3; ++i)
+  // Gs = sum N gov ((i, j, k) - fx)^T dx = (sum N gov (i, j, k)^T - gw fx^T) dx.
+  // With s_n = m gm + (u + A dpos).gov = m gm + (b + i A0 dx + j A1 dx + k A2 dx).gov,
+  // dL/dx = (sum dNx s, sum dNy s, sum dNz s) - A^T gw.  Every sum over the
+  // nodes is taken one axis at a time (z within a row, then y, then x), the
+  // weight and its derivative factors applied per axis.
+  const f3 b = u + a0;
+  f3 gw, si, sj, sk;
+  float gxx, gxy, gxz;
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+  for (int i = 0; i < 3; ++i) {
+    const f3 bi = step3(b, a0c, i);
+    f3 q0, qj, qk;        // over the x-row i: sum w_y w_z gov, sum j w_y w_z gov, sum k w_y w_z gov
+    float t00, t10, t01;  // sum w_y w_z s, sum w1_y w_z s, sum w_y w1_z s
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float Nw = st.w[0][i] * st.w[1][j] * st.w[2][k];
-        const float4 g4 = __ldg(ig + nc.at(i, j, k));
-        const f3 gov = mk3(g4.x, g4.y, g4.z);
-        const f3 gN = mk3(w1[0][i] * st.w[1][j] * st.w[2][k], st.w[0][i] * w1[1][j] * st.w[2][k],
-                          st.w[0][i] * st.w[1][j] * w1[2][k]);
-        const f3 Ad = step3(step3(step3(a0, a0c, i), a1c, j), a2c, k);
-        const f3 a = gov * Nw;
-        gw += a;
-        if (i) si += i == 1 ? a : a * 2.f;
-        if (j) sj += j == 1 ? a : a * 2.f;
-        if (k) sk += k == 1 ? a : a * 2.f;
-        g_x += gN * (g4.w * m + dot(u, gov) + dot(Ad, gov));
+    for (int j = 0; j < 3; ++j) {
+      const f3 bij = step3(bi, a1c, j);
+      const float4 h0 = __ldg(ig + nc.at(i, j, 0)), h1 = __ldg(ig + nc.at(i, j, 1)), h2 = __ldg(ig + nc.at(i, j, 2));
+      const f3 g0 = xyz(h0), g1 = xyz(h1), g2 = xyz(h2);
+      const float s0 = h0.w * m + dot(bij, g0);
+      const float s1 = h1.w * m + dot(bij + a2c, g1);
+      const float s2 = h2.w * m + dot(bij + a2c * 2.f, g2);
+      const f3 t1 = g1 * st.w[2][1];
+      const f3 p0 = g0 * st.w[2][0] + t1 + g2 * st.w[2][2];  // sum_k w_z gov
+      const f3 p1 = t1 + g2 * (2.f * st.w[2][2]);           // sum_k k w_z gov
+      const float S0 = s0 * st.w[2][0] + s1 * st.w[2][1] + s2 * st.w[2][2];
+      const float S1 = s0 * w1[2][0] + s1 * w1[2][1] + s2 * w1[2][2];
+      const float wy = st.w[1][j], dwy = w1[1][j];
+      if (j == 0) {
+        q0 = p0 * wy;
+        qk = p1 * wy;
+        t00 = S0 * wy;
+        t10 = S0 * dwy;
+        t01 = S1 * wy;
+      } else {
+        q0 += p0 * wy;
+        qk += p1 * wy;
+        qj = j == 1 ? p0 * wy : qj + p0 * (2.f * wy);
+        t00 += S0 * wy;
+        t10 += S0 * dwy;
+        t01 += S1 * wy;
       }
-  g_x -= mtv(A, gw);
+    }
+    const float wx = st.w[0][i], dwx = w1[0][i];
+    if (i == 0) {
+      gw = q0 * wx;
+      sj = qj * wx;
+      sk = qk * wx;
+      gxx = t00 * dwx;
+      gxy = t10 * wx;
+      gxz = t01 * wx;
+    } else {
+      gw += q0 * wx;
+      sj += qj * wx;
+      sk += qk * wx;
+      si = i == 1 ? q0 * wx : si + q0 * (2.f * wx);
+      gxx += t00 * dwx;
+      gxy += t10 * wx;
+      gxz += t01 * wx;
+    }
+  }
+  const f3 g_x = mk3(gxx, gxy, gxz) - mtv(A, gw);
   m33 Gs;
   {
     const f3 c0 = (si - gw * st.fx[0]) * E.dx, c1 = (sj - gw * st.fx[1]) * E.dx, c2 = (sk - gw * st.fx[2]) * E.dx;
