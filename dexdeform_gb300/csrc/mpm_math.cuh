@@ -447,15 +447,38 @@ struct Plastic {
   f3 dm1;       // expe - 1 without cancellation
 };
 
+// Whether the return mapping certainly leaves sigma inside the yield surface,
+// decided without logarithms.  For |d| <= 1/2, log1p(d) = d - d^2/2 + t with
+// |t| <= |d|^3 / (3 (1 - |d|)) <= (2/3) |d|^3, so the deviatoric log strain
+// satisfies |eps_hat| <= |dev(d - d^2/2)| + (2/3) sqrt(sum d^6); true when that
+// bound (with the norm's epsilon) is below the yield radius yield / (2 mu) by 0.1%.
+DX_HD bool surely_elastic(f3 d, float mu, float yield) {
+  if (!(fabsf(d.x) <= 0.5f && fabsf(d.y) <= 0.5f && fabsf(d.z) <= 0.5f)) return false;
+  const f3 d2 = hadamard(d, d);
+  const f3 q = d - d2 * 0.5f;
+  const float m = (q.x + q.y + q.z) * (1.f / 3.f);
+  const f3 qh = mk3(q.x - m, q.y - m, q.z - m);
+  const f3 d3 = hadamard(d2, mk3(fabsf(d.x), fabsf(d.y), fabsf(d.z)));
+  const float ub = sqrtf(dot(qh, qh)) + (2.f / 3.f) * sqrtf(dot(d3, d3));
+  const float r = yield / (2.f * mu);
+  return ub * ub + kNormEps < 0.999f * r * r;
+}
+
 DX_HD Plastic constitutive(const SVD3 &sv, const m33 &Ftmp, float mu, float lam, float yield) {
   Plastic o;
-  float e[3], dv[3] = {sv.d.x, sv.d.y, sv.d.z}, sv_[3] = {sv.s.x, sv.s.y, sv.s.z};
+  // log strain e, its deviatoric part and norm; left at zero (not used) when
+  // the state is surely elastic
+  float e[3] = {0.f, 0.f, 0.f}, dg = -1.f, ehn = 1.f;
+  f3 eh = mk3(0.f, 0.f, 0.f);
+  if (!surely_elastic(sv.d, mu, yield)) {
+    const float dv[3] = {sv.d.x, sv.d.y, sv.d.z}, sv_[3] = {sv.s.x, sv.s.y, sv.s.z};
 #pragma unroll
-  for (int i = 0; i < 3; ++i) e[i] = sv_[i] >= kSigClip ? log1pf(dv[i]) : logf(kSigClip);
-  float mean = (e[0] + e[1] + e[2]) * (1.f / 3.f);
-  f3 eh = mk3(e[0] - mean, e[1] - mean, e[2] - mean);
-  float ehn = sqrtf(dot(eh, eh) + kNormEps);
-  float dg = ehn - yield / (2.f * mu);
+    for (int i = 0; i < 3; ++i) e[i] = sv_[i] >= kSigClip ? log1pf(dv[i]) : logf(kSigClip);
+    const float mean = (e[0] + e[1] + e[2]) * (1.f / 3.f);
+    eh = mk3(e[0] - mean, e[1] - mean, e[2] - mean);
+    ehn = sqrtf(dot(eh, eh) + kNormEps);
+    dg = ehn - yield / (2.f * mu);
+  }
   o.eps_hat = eh;
   o.eps_hat_norm = ehn;
   o.delta_gamma = dg;

@@ -74,6 +74,16 @@ def stress_backward(F, C, dt, mly, gP, gF):
     return out, Ft, y.astype(bool)
 
 
+def surely_elastic(d, mu, ys):
+    """The return mapping's logarithm-free elastic test (mpm_math.cuh)."""
+    L = load()
+    d, ys = f32(d), f32(ys)
+    out = np.zeros(d.shape[0], np.int32)
+    L.host_surely_elastic(ctypes.c_int(d.shape[0]), _p(d), ctypes.c_float(mu), _p(ys),
+                          out.ctypes.data_as(ctypes.c_void_p))
+    return out.astype(bool)
+
+
 def substep(env, st, t):
     """One forward substep of workloads.Env `env` from state dict st at substep t."""
     L = load()

@@ -49,6 +49,11 @@ void host_stress_backward(int n, const float *F, const float *C, float dt, const
     yielded[p] = o.yielded ? 1 : 0;
   }
 }
+// the return mapping's logarithm-free elastic test for sigma - 1 = d
+void host_surely_elastic(int n, const float *d, float mu, const float *ys, int *out) {
+  for (int p = 0; p < n; ++p)
+    out[p] = surely_elastic(mk3(d[3 * p], d[3 * p + 1], d[3 * p + 2]), mu, ys[p]) ? 1 : 0;
+}
 // gradient of F_tmp from gradients of (U, sigma, V) for given SVDs (U, sig, d, V)
 void host_svd_backward(int n, const float *U, const float *sig, const float *d, const float *V, const float *gU,
                        const float *gs, const float *gV, const float *gdirect, float *out) {

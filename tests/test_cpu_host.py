@@ -190,6 +190,35 @@ def test_stress_adjoint_matches_finite_differences():
         assert rel(out[k], fd) < 2e-5, (k, bool(yielded[k]), rel(out[k], fd))
 
 
+def test_elastic_pretest_never_skips_a_yield():
+    """The return mapping decides "not yielded" without logarithms when a
+    bound on the deviatoric log strain is inside the yield radius; it must
+    never say so for a state whose exact (FP64) test yields, and it should
+    say so for most states well inside the surface."""
+    import host_math as H
+    rng = np.random.default_rng(8)
+    n = 200000
+    mu = 2083.33
+    ys = rng.uniform(30, 80, n)
+    r = ys / (2 * mu)
+    # deviatoric directions scaled to 0.5x .. 1.5x the yield radius, plus a
+    # volumetric part and some large strains
+    dirs = rng.normal(size=(n, 3))
+    dirs -= dirs.mean(1, keepdims=True)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    scale = rng.uniform(0.5, 1.5, n) * r
+    d = dirs * scale[:, None] + rng.normal(size=(n, 1)) * 0.02
+    d[: n // 10] *= 20.0
+    d = np.clip(d, -0.9, 3.0).astype(np.float32)
+    sure = H.surely_elastic(d, mu, ys)
+    e = np.log1p(d.astype(np.float64))
+    eh = e - e.mean(1, keepdims=True)
+    dg = np.sqrt((eh * eh).sum(1) + 1e-8) - ys.astype(np.float32).astype(np.float64) / (2 * np.float32(mu))
+    assert not (sure & (dg > 0)).any()
+    inside = (dg < -0.05 * r) & (np.abs(d).max(1) < 0.1)   # small strains well inside the surface
+    assert sure[inside].mean() > 0.95
+
+
 def test_host_substep_matches_oracle_off_rest(oracle_mod):
     """The product arithmetic (host build) for one substep from a non-rest
     state meets the 1e-5 bar against the FP64 oracle."""
