@@ -366,11 +366,28 @@ __device__ __forceinline__ int reduce_scatter16_index(int lane) {
   return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
 }
 
-__device__ __forceinline__ void mark_block(const DexBatch &B, int X, int blk) {
-  uint32_t *flag = slot_flags(B, X) + blk;
-  if (*reinterpret_cast<volatile uint32_t *>(flag) == 0u) {
-    if (atomicExch(flag, 1u) == 0u) {
-      int at = atomicAdd(B.block_count + X, 1);
+// Mark the 1 to 8 blocks (2 per axis at most) that a stencil with base b
+// touches as active in slot X, appending newly marked ones to its list.  The
+// flags of all of them are read first (independent loads), then the unmarked
+// ones are claimed with an exchange.
+__device__ __forceinline__ void mark_blocks(const DexBatch &B, const DexEnv &E, int X, const int b[3]) {
+  const int nby = E.gy >> 2, nbz = E.gz >> 2;
+  const int bx = b[0] >> 2, by = b[1] >> 2, bz = b[2] >> 2;
+  const bool ex = ((b[0] + 2) >> 2) != bx, ey = ((b[1] + 2) >> 2) != by, ez = ((b[2] + 2) >> 2) != bz;
+  const int blk0 = E.blk_off + (bx * nby + by) * nbz + bz;
+  uint32_t *flags = slot_flags(B, X);
+  uint32_t f[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const bool use = (!(c & 4) || ex) && (!(c & 2) || ey) && (!(c & 1) || ez);
+    const int blk = blk0 + (((c >> 2) & 1) * nby + ((c >> 1) & 1)) * nbz + (c & 1);
+    f[c] = use ? *reinterpret_cast<volatile uint32_t *>(flags + blk) : 1u;
+  }
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int blk = blk0 + (((c >> 2) & 1) * nby + ((c >> 1) & 1)) * nbz + (c & 1);
+    if (f[c] == 0u && atomicExch(flags + blk, 1u) == 0u) {
+      const int at = atomicAdd(B.block_count + X, 1);
       slot_list(B, X)[at] = blk;
     }
   }
@@ -489,15 +506,7 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
     }
   }
 
-  if (live && R.head) {
-    const int nby = E.gy >> 2, nbz = E.gz >> 2;
-    const int b0x = st.base[0] >> 2, b1x = (st.base[0] + 2) >> 2;
-    const int b0y = st.base[1] >> 2, b1y = (st.base[1] + 2) >> 2;
-    const int b0z = st.base[2] >> 2, b1z = (st.base[2] + 2) >> 2;
-    for (int bx = b0x; bx <= b1x; ++bx)
-      for (int by = b0y; by <= b1y; ++by)
-        for (int bz = b0z; bz <= b1z; ++bz) mark_block(B, X, E.blk_off + (bx * nby + by) * nbz + bz);
-  }
+  if (live && R.head) mark_blocks(B, E, X, st.base);
 }
 
 // P2G of state S into slot X (projected F to Snext, nullable; tape nullable).
