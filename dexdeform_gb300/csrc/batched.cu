@@ -540,6 +540,8 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
   const bool in = loc < E.n;
   const int p = E.p_off + (in ? loc : 0);
   const f3 x = ldf3(S, N, PX, p);
+  // F of state t + 1 (written by the previous P2G), loaded before the gather
+  const m33 F1 = ldm33(Snext, N, PF, p);
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by their P2G
@@ -569,7 +571,7 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
     stf3(Snext, N, PV, p, nv);
     stm33(Snext, N, PC, p, nC);
   }
-  p2g_lane(B, E, Xs, p, ok, nx, nv, ldm33(Snext, N, PF, p), nC, S2, tape, lane);
+  p2g_lane(B, E, Xs, p, ok, nx, nv, F1, nC, S2, tape, lane);
 }
 
 // ============================================================ grid update
@@ -611,9 +613,18 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, i
     bz = local % nbz;
   };
   const int stride = gridDim.x * per_cta;
-  for (int item = blockIdx.x * per_cta + sub; item < cnt; item += stride) {
-    const int blk = list[item];
-    const DexEnv E = B.envs[B.block_env[blk]];
+  // the list entries of the next two items and the env of the next one are
+  // loaded while this item is processed (each load's address is known then)
+  int item = blockIdx.x * per_cta + sub;
+  int blk_a = item < cnt ? list[item] : 0;
+  int blk_b = item + stride < cnt ? list[item + stride] : 0;
+  int env_a = item < cnt ? B.block_env[blk_a] : 0;
+  for (; item < cnt; item += stride) {
+    const int blk = blk_a, env = env_a;
+    env_a = item + stride < cnt ? B.block_env[blk_b] : 0;
+    blk_a = blk_b;
+    blk_b = item + 2 * stride < cnt ? list[item + 2 * stride] : 0;
+    const DexEnv E = B.envs[env];
     int bx, by, bz;
     coords(E, blk, bx, by, bz);
     const int ci = (blk << 6) + cell;
