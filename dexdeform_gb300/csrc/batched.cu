@@ -431,8 +431,19 @@ __device__ __forceinline__ uint32_t bodies_near_block(const DexBatch &B, const D
 // projected F (to Fout's F planes), the tape, and the APIC momentum + stress
 // scatter into grid slot X, marking the blocks the stencil touches.  `live`
 // lanes contribute; every lane of the warp calls it.
+// Per-particle material: mass, volume, mu, lambda, yield stress.
+struct Material {
+  float m, vol, mu, lam, ys;
+};
+__device__ __forceinline__ Material load_material(const DexBatch &B, int p) {
+  const int N = B.n_particles;
+  return Material{__ldg(B.mass + p), __ldg(B.vol + p), __ldg(B.mu_lam_yield + p), __ldg(B.mu_lam_yield + N + p),
+                  __ldg(B.mu_lam_yield + 2 * N + p)};
+}
+
 __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int X, int p, bool live, f3 x, f3 v,
-                                         const m33 &F, const m33 &C, float *Fout, float *tape, int lane) {
+                                         const m33 &F, const m33 &C, const Material &mat, float *Fout, float *tape,
+                                         int lane) {
   const int N = B.n_particles;
   Stencil st;
   make_stencil(x, E.inv_dx, st);
@@ -449,10 +460,8 @@ __device__ __forceinline__ void p2g_lane(const DexBatch &B, const DexEnv &E, int
   float *red = warp_red_buffer();
   const Ranked R = rank_lanes(key, lane);
 
-  const float m = live ? __ldg(B.mass + p) : 0.f;
-  const float vol = __ldg(B.vol + p);
-  const float mu = __ldg(B.mu_lam_yield + p), lam = __ldg(B.mu_lam_yield + N + p),
-              ys = __ldg(B.mu_lam_yield + 2 * N + p);
+  const float m = live ? mat.m : 0.f;
+  const float vol = mat.vol, mu = mat.mu, lam = mat.lam, ys = mat.ys;
   const m33 Et = deviation_tmp(F, C, E.dt);
   const SVD3 sv = svd3_from_deviation(Et);
   m33 Ft = Et;
@@ -520,8 +529,8 @@ __global__ void __launch_bounds__(256, DEX_P2G_MINB) k_p2g(DexBatch B, int X, co
   const int loc = first + threadIdx.x;
   const bool in = loc < E.n;
   const int p = E.p_off + (in ? loc : 0);
-  p2g_lane(B, E, X, p, in, ldf3(S, N, PX, p), ldf3(S, N, PV, p), ldm33(S, N, PF, p), ldm33(S, N, PC, p), Snext, tape,
-           lane);
+  p2g_lane(B, E, X, p, in, ldf3(S, N, PX, p), ldf3(S, N, PV, p), ldm33(S, N, PF, p), ldm33(S, N, PC, p),
+           load_material(B, p), Snext, tape, lane);
 }
 
 // G2P of substep t fused with P2G of substep t + 1 (integrator.cu:1059-1109
@@ -571,7 +580,7 @@ __global__ void __launch_bounds__(256, DEX_G2P2G_MINB) k_g2p2g(DexBatch B, int X
     stf3(Snext, N, PV, p, nv);
     stm33(Snext, N, PC, p, nC);
   }
-  p2g_lane(B, E, Xs, p, ok, nx, nv, F1, nC, S2, tape, lane);
+  p2g_lane(B, E, Xs, p, ok, nx, nv, F1, nC, load_material(B, p), S2, tape, lane);
 }
 
 // ============================================================ grid update
@@ -1137,6 +1146,7 @@ __global__ void __launch_bounds__(128, DEX_P2G2G_GRAD_MINB) k_p2g2g_grad(DexBatc
   const bool in = loc < E.n;
   const int p = E.p_off + (in ? loc : 0);
   const f3 x = ldf3(S, N, PX, p);
+  const f3 xprev = ldf3(Sprev, N, PX, p);  // for the G2P adjoint, loaded ahead
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by the G2P adjoint
@@ -1150,7 +1160,7 @@ __global__ void __launch_bounds__(128, DEX_P2G2G_GRAD_MINB) k_p2g2g_grad(DexBatc
     gx = gv = mk3(0.f, 0.f, 0.f);
     gC = mzero();
   }
-  g2p_grad_lane(B, E, Xprev, p, in, ldf3(Sprev, N, PX, p), v, gx, gv, gC, Gprev, lane);
+  g2p_grad_lane(B, E, Xprev, p, in, xprev, v, gx, gv, gC, Gprev, lane);
 }
 
 // Zero the grid cells and flags of the listed blocks of slots [first, last)
