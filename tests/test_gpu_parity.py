@@ -419,15 +419,15 @@ def test_fused_substeps_equal_unfused(cuda):
         assert rel(other.cpu().numpy(), finals[0].cpu().numpy()) < 1e-4
 
 
-def test_fused_adjoint_equals_unfused(cuda):
+@pytest.mark.parametrize("T", [1, 2, 10])
+def test_fused_adjoint_equals_unfused(cuda, T):
     """BatchEngine.run_adjoint (each P2G adjoint fused with the previous
     substep's G2P adjoint, the x, v, C gradients passed in registers) against
     the same T adjoint substeps launched one kernel at a time, after the same
-    kept forward with a tape."""
+    kept forward with a tape (T = 1: no fused launch; T = 2: one)."""
     from dexdeform_gb300 import workloads as W
     from dexdeform_gb300.engine import BatchEngine, EnvSpec
     envs = W.batch_envs(7, n_envs=3, steps=10, n_lo=500, n_hi=3000)
-    T = 10
     outs = []
     for mode in ("unfused", "fused"):
         E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=T + 2)
