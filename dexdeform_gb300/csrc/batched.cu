@@ -107,19 +107,37 @@ __device__ __forceinline__ void prefetch_plane(const float *plane, int p0, int p
 // P2G adjoint reads them instead of repeating the SVD and return mapping.
 constexpr int kTapePlanes = 33;
 static_assert(kTapePlanes == DEXMPM_TAPE_PLANES, "tape layout");
+// The tape is written with streaming stores and read once with evict-first
+// loads: it is consumed by the adjoint long after it is written, so it should
+// not displace the grid slots and states the next substeps reuse from L2.
+__device__ __forceinline__ void tape_put(float *T, int N, int plane, int p, float v) {
+  __stcs(T + (size_t)plane * N + p, v);
+}
+__device__ __forceinline__ float tape_get(const float *T, int N, int plane, int p) {
+  return __ldcs(T + (size_t)plane * N + p);
+}
 __device__ __forceinline__ void store_tape(float *T, int N, int p, const SVD3 &sv, const m33 &P) {
-  stm33(T, N, 0, p, sv.U);
-  stm33(T, N, 9, p, sv.V);
-  stf3(T, N, 18, p, sv.s);
-  stf3(T, N, 21, p, sv.d);
-  stm33(T, N, 24, p, P);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    tape_put(T, N, i, p, sv.U.a[i / 3][i % 3]);
+    tape_put(T, N, 9 + i, p, sv.V.a[i / 3][i % 3]);
+    tape_put(T, N, 24 + i, p, P.a[i / 3][i % 3]);
+  }
+  tape_put(T, N, 18, p, sv.s.x); tape_put(T, N, 19, p, sv.s.y); tape_put(T, N, 20, p, sv.s.z);
+  tape_put(T, N, 21, p, sv.d.x); tape_put(T, N, 22, p, sv.d.y); tape_put(T, N, 23, p, sv.d.z);
+}
+__device__ __forceinline__ m33 tape_m33(const float *T, int N, int plane, int p) {
+  m33 m;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m.a[i / 3][i % 3] = tape_get(T, N, plane + i, p);
+  return m;
 }
 __device__ __forceinline__ SVD3 load_svd(const float *__restrict__ T, int N, int p) {
   SVD3 sv;
-  sv.U = ldm33(T, N, 0, p);
-  sv.V = ldm33(T, N, 9, p);
-  sv.s = ldf3(T, N, 18, p);
-  sv.d = ldf3(T, N, 21, p);
+  sv.U = tape_m33(T, N, 0, p);
+  sv.V = tape_m33(T, N, 9, p);
+  sv.s = mk3(tape_get(T, N, 18, p), tape_get(T, N, 19, p), tape_get(T, N, 20, p));
+  sv.d = mk3(tape_get(T, N, 21, p), tape_get(T, N, 22, p), tape_get(T, N, 23, p));
   return sv;
 }
 
@@ -962,7 +980,7 @@ __device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEn
     pl = constitutive(sv, Ft, mu, lam, ys);
   };
   if constexpr (kTape) {
-    P = ldm33(tape, N, 24, p);
+    P = tape_m33(tape, N, 24, p);
   } else {
     forward_state();
     P = pl.P;

@@ -204,7 +204,7 @@ def test_svd_tape_matches_recomputed_svd(cuda):
     outs = []
     for use_tape in (True, False):
         bg = torch.zeros((2, nb, 8), device="cuda")
-        g = torch.empty_like(s0)
+        g = torch.zeros_like(s0)
         E.substep(s0, s1, poses[0], poses[1], slot=2, tape=tape if use_tape else None)
         E.substep_grad(s0, s1, g_next, g, poses[0], poses[1], bg[0], bg[1], slot=2,
                        tape=tape if use_tape else None)
