@@ -33,11 +33,12 @@ using namespace dexmpm;
 
 // Compile-time tuning knobs.  Defaults were picked by timing every kernel on
 // GB300 over the 64-env batch: minimum resident CTAs per SM (register caps:
-// P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint 128, the fused
-// adjoint 96 (5 CTAs of 128 per SM), grid update and its adjoint 64 -- four 256-thread CTAs per SM, so that
-// the persistent grid kernels cover the active blocks in fewer rounds) and
-// the unrolling of the outer loop over the 27 stencil nodes in the adjoints
-// (full unrolling keeps the weight arrays out of local memory).
+// P2G and fused G2P/P2G 85, G2P adjoint 85, P2G adjoint 128, the fused adjoint
+// 96 -- five 128-thread CTAs per SM --, grid update and its adjoint 64 -- four
+// 256-thread CTAs per SM, so that the persistent grid kernels cover the
+// active blocks in fewer rounds) and the unrolling of the outer loop over the
+// 27 stencil nodes in the adjoints (full unrolling keeps the weight arrays out
+// of local memory).
 #ifndef DEX_P2G_MINB
 #define DEX_P2G_MINB 3
 #endif
