@@ -431,8 +431,8 @@ ALG_BYTES = {
 
 # DRAM bytes (read + write) per particle of one launch, from ncu captures
 # on the 64-env batch (profiles/k_*_batch64.md)
-NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 143.818752e6 / 654552,
-                               "g2p2g": 63.61984e6 / 654552, "p2g2g_grad": 236.897024e6 / 654552}
+NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 144.833024e6 / 654552,
+                               "g2p2g": 63.928576e6 / 654552, "p2g2g_grad": 234.343168e6 / 654552}
 
 # launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
