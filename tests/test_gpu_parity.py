@@ -83,7 +83,7 @@ def test_batched_forward_from_rest_with_contacts(cuda, oracle_mod):
         assert rel(got[20][k], z[f"s20_{k}"]) < 1e-3, k
 
 
-def test_batched_forward_one_substep_north_star(cuda, oracle_mod):
+def test_batched_forward_one_substep_within_1e5(cuda, oracle_mod):
     """From a non-rest state: every field within 1e-5 after one substep."""
     from dexdeform_gb300 import workloads as W
     for seed in (0, 5):
