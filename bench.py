@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="backward without recomputing env step k - 1 on a second stream during the adjoint of k")
     return ap.parse_args()
 
 
@@ -186,8 +188,10 @@ def run_ours(args, rank, world, local):
     envs = build_batch(rank, args.envs)
     n_total = sum(e.n for e in envs)
     work = n_total * SUBSTEPS * ENV_STEPS  # particle-substeps per rollout
-    E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True, grid_slots=SUBSTEPS + 2)
-    R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS)
+    # two sets of kept grid slots: the backward recomputes env step k - 1
+    # while the adjoint of env step k runs
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True, grid_slots=2 * SUBSTEPS + 2)
+    R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS, overlap=not args.no_overlap)
     poses_h = E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs])
     R.poses.copy_(torch.from_numpy(poses_h))
     s0 = E.pack_state([e.state() for e in envs])
@@ -289,6 +293,7 @@ def run_ours(args, rank, world, local):
     kt, cells = kernel_times(E, R, s0, g_final)
     roof = roofline(E, kt, cells)
     err = E.error_word()
+    overlapped = R.overlap
 
     plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
     cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs, budget_s=12.0)
@@ -309,6 +314,8 @@ def run_ours(args, rank, world, local):
                        "n_envs": len(envs), "particles_per_replica": n_total, "substeps": SUBSTEPS * ENV_STEPS,
                        "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
                        "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1], "source": "autotune"},
+                       "backward": ("recompute of env step k-1 on a second stream during the adjoint of env step k"
+                                    if overlapped else "recompute, then adjoint, per env step"),
                        "l2": "inputs larger than L2 (per-step state traffic ~4 GB >> 129 MB L2)"},
             "fwd": {"value": fwd_value, "unit": UNIT, "ms_per_step": fwd_ms / args.steps},
             "latency_ms": {"p50": ps[len(ps) // 2], "p99": ps[min(len(ps) - 1, int(math.ceil(0.99 * len(ps))) - 1)],
@@ -507,7 +514,7 @@ def large_env_leg(dev, substeps=100, env_steps=10):
     env = W.large_env(0, steps=substeps * env_steps)
     base = torch.cuda.memory_allocated(dev)
     torch.cuda.reset_peak_memory_stats(dev)
-    E = BatchEngine([EnvSpec.from_env(env)], device=dev, grad=True, grid_slots=substeps + 2)
+    E = BatchEngine([EnvSpec.from_env(env)], device=dev, grad=True, grid_slots=2 * substeps + 2)
     R = Rollout(E, substeps=substeps, env_steps=env_steps)
     R.poses.copy_(torch.from_numpy(E.pack_poses([env.poses[:, :, :3]], [env.poses[:, :, 3:]])))
     s0 = E.pack_state([env.state()])

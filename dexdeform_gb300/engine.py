@@ -253,13 +253,13 @@ class BatchEngine:
         return slot
 
     def run_substeps(self, sts: Sequence[torch.Tensor], poses: torch.Tensor, kept: bool = False,
-                     tapes: Optional[torch.Tensor] = None):
+                     tapes: Optional[torch.Tensor] = None, slot_base: int = 2):
         """T = len(sts) - 1 forward substeps from sts[0] to sts[T] (sts[t], 0 < t
         < T, hold the intermediate states; sts[t] and sts[t + 2] may be one
         buffer), with body poses poses[0..T].  The G2P of every substep but
         the last is fused with the next substep's P2G.  Slots: the forward
-        pair (kept=False) or slot 2 + t kept for the adjoint of substep t
-        (kept=True), with tapes[t] written when given."""
+        pair (kept=False) or slot slot_base + t kept for the adjoint of substep
+        t (kept=True), with tapes[t] written when given."""
         T = len(sts) - 1
         if T < 1:
             return
@@ -267,8 +267,8 @@ class BatchEngine:
 
         def take(t):
             if kept:
-                assert 2 + t < self.n_grid_slots
-                return 2 + t, -1
+                assert 2 <= slot_base and slot_base + t < self.n_grid_slots
+                return slot_base + t, -1
             slot = self.fslot
             self.fslot ^= 1
             return slot, slot ^ 1
@@ -313,9 +313,9 @@ class BatchEngine:
         self.launches += 3
 
     def run_adjoint(self, sts: Sequence[torch.Tensor], g_next: torch.Tensor, g: torch.Tensor, poses: torch.Tensor,
-                    bgrad: torch.Tensor, tapes: Optional[torch.Tensor] = None) -> torch.Tensor:
+                    bgrad: torch.Tensor, tapes: Optional[torch.Tensor] = None, slot_base: int = 2) -> torch.Tensor:
         """Adjoint of the T = len(sts) - 1 substeps that run_substeps(kept=True)
-        ran from sts[0] (grid slots 2..T+1, tapes[t] when given), from the
+        ran from sts[0] (grid slots slot_base..slot_base+T-1, tapes[t] when given), from the
         gradient of sts[T] in g_next; g is scratch of the same shape.  The P2G
         adjoint of every substep but the first is fused with the G2P adjoint
         of the substep before it.  Returns the buffer (g_next or g) that holds
@@ -323,25 +323,27 @@ class BatchEngine:
         bgrad[t].  Clears the slots."""
         assert self.grad, "engine built without gradient buffers"
         T = len(sts) - 1
-        assert T >= 1 and 2 + T <= self.n_grid_slots
+        assert T >= 1 and 2 <= slot_base and slot_base + T <= self.n_grid_slots
         L, bp, sp = self.lib, self._bp, N.stream_ptr()
 
         def tape(t):
             return N.ptr(tapes[t]) if tapes is not None else None
 
+        b0 = slot_base
         s = T - 1
-        N.check(L.dexmpm_g2p_grad(bp, 2 + s, N.ptr(sts[s]), N.ptr(sts[s + 1]), N.ptr(g_next), N.ptr(g), sp),
+        N.check(L.dexmpm_g2p_grad(bp, b0 + s, N.ptr(sts[s]), N.ptr(sts[s + 1]), N.ptr(g_next), N.ptr(g), sp),
                 "dexmpm_g2p_grad")
         for s in range(T - 1, -1, -1):
-            N.check(L.dexmpm_grid_op_grad(bp, 2 + s, N.ptr(poses[s]), N.ptr(poses[s + 1]), N.ptr(bgrad[s]),
+            N.check(L.dexmpm_grid_op_grad(bp, b0 + s, N.ptr(poses[s]), N.ptr(poses[s + 1]), N.ptr(bgrad[s]),
                                           N.ptr(bgrad[s + 1]), sp), "dexmpm_grid_op_grad")
             if s > 0:
                 # gradients: of state s + 1 in g_next, of state s in g; the x
                 # gradient of state s - 1 goes to g_next
-                N.check(L.dexmpm_p2g_g2p_grad(bp, 2 + s, 1 + s, N.ptr(sts[s]), N.ptr(sts[s - 1]), N.ptr(g_next),
-                                              N.ptr(g), N.ptr(g_next), tape(s), sp), "dexmpm_p2g_g2p_grad")
+                N.check(L.dexmpm_p2g_g2p_grad(bp, b0 + s, b0 + s - 1, N.ptr(sts[s]), N.ptr(sts[s - 1]),
+                                              N.ptr(g_next), N.ptr(g), N.ptr(g_next), tape(s), sp),
+                        "dexmpm_p2g_g2p_grad")
             else:
-                N.check(L.dexmpm_p2g_grad(bp, 2, N.ptr(sts[0]), N.ptr(g_next), N.ptr(g), tape(0), sp),
+                N.check(L.dexmpm_p2g_grad(bp, b0, N.ptr(sts[0]), N.ptr(g_next), N.ptr(g), tape(0), sp),
                         "dexmpm_p2g_grad")
             g_next, g = g, g_next
         self.launches += 2 * T + 1
@@ -384,11 +386,14 @@ class Rollout:
     grids and the adjoint reads them; otherwise the adjoint recomputes P2G and
     the grid update per substep.  With kept grids, the forward pass runs its
     last env step the way the backward would recompute it (kept slots, tape),
-    so the backward of that env step needs no recompute.  Each env step's
-    forward and backward are captured as CUDA graphs on first use and
-    replayed afterwards."""
+    so the backward of that env step needs no recompute.  With 2 T + 2 grid
+    slots (and `overlap`), the backward keeps two sets of slots, tapes and
+    state rings and recomputes env step k - 1 on a second stream while the
+    adjoint of env step k runs.  Each env step's forward, recompute and
+    adjoint are captured as CUDA graphs on first use and replayed afterwards."""
 
-    def __init__(self, engine: BatchEngine, substeps: int, env_steps: int, use_graphs: bool = True):
+    def __init__(self, engine: BatchEngine, substeps: int, env_steps: int, use_graphs: bool = True,
+                 overlap: bool = True):
         self.E = engine
         self.T, self.S = int(substeps), int(env_steps)
         self.use_graphs = use_graphs
@@ -396,6 +401,7 @@ class Rollout:
         nb = max(engine.n_bodies, 1)
         self.poses = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
         self.keep_grids = engine.n_grid_slots >= self.T + 2
+        self.overlap = bool(overlap) and engine.grad and engine.n_grid_slots >= 2 * self.T + 2
         self.tape = None
         if engine.grad:
             self.ckpt = engine.new_slots(self.S + 1)
@@ -407,6 +413,11 @@ class Rollout:
         else:
             self.ckpt = engine.new_slots(2)
             self.ring = engine.new_slots(2)
+        # slot sets of the overlapped backward: (first kept grid slot, state ring, tape)
+        self._sets = [(2, self.ring, self.tape)]
+        if self.overlap:
+            self._sets.append((2 + self.T, engine.new_slots(self.T + 1), engine.new_tape(self.T)))
+            self._side = torch.cuda.Stream(device=dev)
         self._fwd_graphs, self._bwd_graphs = {}, {}
         self._kept_live = False  # slots 2..T+1 and the tape hold the last env step's forward
 
@@ -506,11 +517,69 @@ class Rollout:
         assert self.E.grad
         self.bgrad.zero_()
         self.gbuf[1].copy_(g_final)
+        if self.overlap and self.S > 1:
+            self._backward_overlapped(on_boundary)
+            return self.gbuf[1]
         for k in range(self.S - 1, -1, -1):
             self.backward_step(k)
             if on_boundary is not None:
                 on_boundary(k, self.gbuf[1])
         return self.gbuf[1]
+
+    # ------------------------------------------------- overlapped backward
+    def _set_of(self, k: int):
+        """Slot set of env step k: the last env step uses set 0 (where the
+        kept forward left it), earlier ones alternate."""
+        return self._sets[(self.S - 1 - k) % 2]
+
+    def _recompute(self, k: int):
+        """Env step k recomputed from ckpt[k] into its slot set (states in the
+        set's ring, grids kept, tape written)."""
+        T = self.T
+        base, ring, tape = self._set_of(k)
+        sts = [self.ckpt[k]] + [ring[t] for t in range(1, T + 1)]
+        self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=tape, slot_base=base)
+
+    def _adjoint(self, k: int):
+        """Adjoint of env step k from its slot set; gradient of ckpt[k+1] in
+        gbuf[1] in, gradient of ckpt[k] in gbuf[1] out."""
+        T = self.T
+        base, ring, tape = self._set_of(k)
+        sts = [self.ckpt[k]] + [ring[t] for t in range(1, T)] + [self.ckpt[k + 1]]
+        out = self.E.run_adjoint(sts, self.gbuf[1], self.gbuf[0], self.poses[k * T:k * T + T + 1],
+                                 self.bgrad[k * T:k * T + T + 1], tapes=tape, slot_base=base)
+        if out is not self.gbuf[1]:
+            self.gbuf[1].copy_(out)
+
+    def _backward_overlapped(self, on_boundary):
+        """Env steps S-1 .. 0: the adjoint of env step k on the current stream
+        while env step k - 1 is recomputed into the other slot set on a side
+        stream.  The recompute of k - 1 starts after everything issued before
+        the adjoint of k (so the adjoint of k + 1, the last user of that set,
+        is done); the adjoint of k waits for the recompute of k."""
+        main, side = torch.cuda.current_stream(), self._side
+        k = self.S - 1
+        if self._kept_live:
+            self._kept_live = False  # the adjoint below consumes the kept slots
+        else:
+            run_graph(self.E, self._bwd_graphs, ("rec", k), lambda: self._recompute(k), self.use_graphs)
+        ready = None
+        for k in range(self.S - 1, -1, -1):
+            nxt = None
+            if k > 0:
+                side.wait_stream(main)
+                with torch.cuda.stream(side):
+                    run_graph(self.E, self._bwd_graphs, ("rec", k - 1), lambda: self._recompute(k - 1),
+                              self.use_graphs)
+                nxt = torch.cuda.Event()
+                nxt.record(side)
+            if ready is not None:
+                main.wait_event(ready)
+            run_graph(self.E, self._bwd_graphs, ("adj", k), lambda: self._adjoint(k), self.use_graphs)
+            if on_boundary is not None:
+                on_boundary(k, self.gbuf[1])
+            ready = nxt
+        main.wait_stream(side)
 
     # -------------------------------------------------------------- graphs
     def _run(self, cache, k, fn):

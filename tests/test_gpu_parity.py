@@ -360,7 +360,10 @@ def test_kept_last_env_step_equals_recompute(cuda):
     envs = W.batch_envs(5, n_envs=3, steps=30, n_lo=500, n_hi=3000)
     T, S = 10, 3
     outs = []
-    for slots, pattern in ((2, "fb"), (T + 2, "fb"), (T + 2, "ffb"), (T + 2, "fnb")):
+    # 2 T + 2 slots: the backward recomputes env step k - 1 on a second
+    # stream while the adjoint of env step k runs (two slot sets)
+    for slots, pattern in ((2, "fb"), (T + 2, "fb"), (T + 2, "ffb"), (T + 2, "fnb"), (2 * T + 2, "fb"),
+                           (2 * T + 2, "ffb"), (2 * T + 2, "fnb")):
         E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=slots)
         R = Rollout(E, substeps=T, env_steps=S)
         R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs],
