@@ -300,6 +300,38 @@ def test_block_culling_never_skips_a_touching_body():
     assert touched.sum() > 1000 and (~may).sum() > 0.3 * n
 
 
+def test_fused_adjoint_entry_checks_arguments(native_lib):
+    """dexmpm_p2g_g2p_grad rejects a missing or gradient-less batch, aliased
+    gradient buffers and bad slots before any CUDA call, and returns OK
+    without a launch for a batch with no particle tiles (the descriptor's
+    pointers are placeholders that are never dereferenced on these paths)."""
+    import ctypes
+    from dexdeform_gb300 import _native as N
+    one = ctypes.c_void_p(1)
+    two, three, four = ctypes.c_void_p(2), ctypes.c_void_p(3), ctypes.c_void_p(4)
+    b = N.DexBatch()
+    for f, _ in N.DexBatch._fields_:
+        if f not in ("n_envs", "n_particles", "n_tiles", "n_blocks", "n_bodies", "tile_size", "grid_ctas", "flags",
+                     "n_slots", "pad0", "pad1", "pad2"):
+            setattr(b, f, 1)
+    b.n_envs, b.n_particles, b.n_tiles, b.n_blocks, b.n_bodies = 1, 32, 1, 8, 0
+    b.tile_size, b.grid_ctas, b.n_slots = 128, 8, 6
+    f = native_lib.dexmpm_p2g_g2p_grad
+    bp = ctypes.byref(b)
+    ARG = 1
+    assert f(None, 3, 2, one, two, three, four, one, None, None) == ARG                   # no batch
+    assert f(bp, 3, 2, one, two, three, four, four, None, None) == ARG                    # g_prev == g
+    assert f(bp, 3, 2, one, two, three, three, one, None, None) == ARG                    # g == g_next
+    assert f(bp, 3, 3, one, two, three, four, one, None, None) == ARG                     # same slot
+    assert f(bp, 6, 2, one, two, three, four, one, None, None) == ARG                     # slot out of range
+    assert f(bp, 3, 2, None, two, three, four, one, None, None) == ARG                    # no state
+    b.vout_grad = None
+    assert f(bp, 3, 2, one, two, three, four, one, None, None) == ARG                     # no gradient grids
+    b.vout_grad = 1
+    b.n_tiles = 0
+    assert f(bp, 3, 2, one, two, three, four, three, None, None) == 0                     # g_prev may be g_next
+
+
 def test_render_launchers_reject_bad_arguments(native_lib):
     """Argument checks of particle_sdf / render run before any CUDA call."""
     import ctypes
