@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-overlap", action="store_true",
                     help="backward without recomputing env step k - 1 on a second stream during the adjoint of k")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
+    ap.add_argument("--presorted", action="store_true",
+                    help="particles handed over already ordered by grid cell (default: sampling order)")
+    ap.add_argument("--serving-requests", type=int, default=200)
     return ap.parse_args()
 
 
@@ -168,9 +172,9 @@ def peaks():
 
 
 # ------------------------------------------------------------- workloads
-def build_batch(seed, n_envs):
+def build_batch(seed, n_envs, presorted=False):
     from dexdeform_gb300 import workloads as W
-    return W.batch_envs(seed, n_envs=n_envs, steps=SUBSTEPS * ENV_STEPS)
+    return W.batch_envs(seed, n_envs=n_envs, steps=SUBSTEPS * ENV_STEPS, sort=presorted)
 
 
 def targets_for(envs):
@@ -185,7 +189,7 @@ def run_ours(args, rank, world, local):
     from dexdeform_gb300 import _native as N
 
     dev = torch.device("cuda", local)
-    envs = build_batch(rank, args.envs)
+    envs = build_batch(rank, args.envs, args.presorted)
     n_total = sum(e.n for e in envs)
     work = n_total * SUBSTEPS * ENV_STEPS  # particle-substeps per rollout
     # two sets of kept grid slots: the backward recomputes env step k - 1
@@ -202,7 +206,7 @@ def run_ours(args, rank, world, local):
         counts[E.p_off[e]:E.p_off[e] + env.n] = 1.0 / env.n
     g_final = torch.zeros_like(s0)
     from dexdeform_gb300.autotune import tune
-    tuned = tune(E, s0, R.poses[:4], use_cache=False)
+    tuned = (E.tile_size, E.grid_ctas) if args.no_tune else tune(E, s0, R.poses[:4], use_cache=False)
 
     def loss_grad(final):
         # L = sum_e mean_p |x - target|^2 ; dL/dx = 2 (x - target) / n_e
@@ -296,9 +300,9 @@ def run_ours(args, rank, world, local):
     overlapped = R.overlap
 
     plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
-    cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs, budget_s=12.0)
+    cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs)
     del R, E
-    serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank)
+    serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank, n_req=args.serving_requests)
     large = None if (args.no_large or world > 1) else large_env_leg(dev)
     rend = None if (args.no_render or world > 1) else render_leg(dev, cpu=not args.no_cpu)
 
@@ -313,7 +317,9 @@ def run_ours(args, rank, world, local):
                                    "checkpoints, CUDA graphs",
                        "n_envs": len(envs), "particles_per_replica": n_total, "substeps": SUBSTEPS * ENV_STEPS,
                        "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
-                       "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1], "source": "autotune"},
+                       "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1],
+                                        "source": "default" if args.no_tune else "autotune"},
+                       "particle_order": "presorted by grid cell" if args.presorted else "sampling order",
                        "backward": ("recompute of env step k-1 on a second stream during the adjoint of env step k"
                                     if overlapped else "recompute, then adjoint, per env step"),
                        "l2": "inputs larger than L2 (per-step state traffic ~4 GB >> 129 MB L2)"},
@@ -440,6 +446,18 @@ ALG_BYTES = {
 # on the 64-env batch (profiles/k_*_batch64.md)
 NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 144.833024e6 / 654552,
                                "g2p2g": 63.928576e6 / 654552, "p2g2g_grad": 234.343168e6 / 654552}
+# L2 reduction traffic and the busy fraction of the L2 atomic units of one
+# launch, from an ncu capture on the same batch (profiles/l2_atomics_batch64.md):
+# (lts__t_requests_op_red.sum, lts__t_sectors_op_red.sum,
+#  lts__d_atomic_input_cycles_active.avg.pct_of_peak_sustained_elapsed)
+NCU_L2_RED = {}
+
+# kernel function of each timed launch variant (the forward pass and the
+# recompute launch the same function, the recompute with the tape written)
+FUNCTION = {"p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape": "k_g2p2g",
+            "grid_op": "k_grid_op", "grid_op_keep": "k_grid_op", "g2p": "k_g2p", "g2p_grad": "k_g2p_grad",
+            "grid_op_grad": "k_grid_op_grad", "p2g_grad": "k_p2g_grad", "p2g2g_grad": "k_p2g2g_grad"}
+
 
 # launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
@@ -450,27 +468,49 @@ def launches_per_substep(T):
 
 
 def roofline(E, kt, cells):
-    import torch
+    """Roofline of the dominant kernel function: the one with the largest
+    device time per fwd+bwd substep, its launch variants combined (achieved =
+    the variants' algorithmic bytes / their device time, both weighted by
+    launches per substep)."""
     peak, src = peaks()
-    # dominant kernel: largest device time per fwd+bwd substep (G2P runs in
-    # both the forward pass and the recompute)
     w = launches_per_substep(SUBSTEPS)
-    per_substep = {k: v * w[k] for k, v in kt.items()}
-    top = max(per_substep, key=per_substep.get)
     n = sum(s.n for s in E.specs)
-    bp, bc = ALG_BYTES[top]
-    alg = bp * n + bc * cells
-    achieved = alg / (kt[top] * 1e-6) / 1e9
-    return {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": src, "alg_bytes_per_launch": int(alg),
-            "avg_launch_us": kt[top],
-            "traffic": int(NCU_DRAM_BYTES_PER_PARTICLE[top] * n) if top in NCU_DRAM_BYTES_PER_PARTICLE else None,
-            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the kernel on the "
-                            "same 64-env batch (654,552 particles, 5 substeps per env step), per particle x n; "
-                            "profiles/k_<kernel>_batch64.md"}
+    per_fn, bytes_fn, launches_fn, traffic_fn, variants = {}, {}, {}, {}, {}
+    for k, us in kt.items():
+        f = FUNCTION[k]
+        bp, bc = ALG_BYTES[k]
+        per_fn[f] = per_fn.get(f, 0.0) + us * w[k]
+        bytes_fn[f] = bytes_fn.get(f, 0.0) + (bp * n + bc * cells) * w[k]
+        launches_fn[f] = launches_fn.get(f, 0.0) + w[k]
+        if k in NCU_DRAM_BYTES_PER_PARTICLE and traffic_fn.get(f, 0.0) is not None:
+            traffic_fn[f] = traffic_fn.get(f, 0.0) + NCU_DRAM_BYTES_PER_PARTICLE[k] * n * w[k]
+        else:
+            traffic_fn[f] = None
+        variants.setdefault(f, {})[k] = {"us": round(us, 2), "launches_per_substep": round(w[k], 4),
+                                         "alg_bytes": int(bp * n + bc * cells)}
+    top = max(per_fn, key=per_fn.get)
+    total = sum(per_fn.values())
+    achieved = bytes_fn[top] / (per_fn[top] * 1e-6) / 1e9
+    L = launches_fn[top]
+    out = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_source": src, "alg_bytes_per_launch": int(bytes_fn[top] / L),
+           "avg_launch_us": per_fn[top] / L, "share_of_substep": per_fn[top] / total,
+           "traffic": int(traffic_fn[top] / L) if traffic_fn.get(top) is not None else None,
+           "variants": variants[top],
+           "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of ncu captures of each launch variant on "
+                           "the same 64-env batch (654,552 particles, 5 substeps per env step), per particle x n, "
+                           "averaged over the variants by launches per substep; profiles/k_<kernel>_batch64.md"}
+    red = [NCU_L2_RED[k] for k in variants[top] if k in NCU_L2_RED]
+    if red:
+        out["atomics"] = {"l2_red_requests_per_launch": int(np.mean([r[0] for r in red])),
+                          "l2_red_sectors_per_launch": int(np.mean([r[1] for r in red])),
+                          "l2_atomic_unit_busy_pct": round(float(np.mean([r[2] for r in red])), 2),
+                          "source": "ncu lts__t_requests_op_red / lts__t_sectors_op_red / "
+                                    "lts__d_atomic_input_cycles_active (profiles/l2_atomics_batch64.md)"}
+    return out
 
 
-def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
+def serving_leg(dev, seed=0, n_req=200, rate_hz=20.0):
     """Continuous-batching server on the serving workload: Poisson arrivals,
     grids 48/64/96^3, particles log-uniform in [2,000, 50,000], horizons
     uniform in [5, 100] env steps x 50 substeps, 30% gradient requests, HBM
@@ -497,6 +537,7 @@ def serving_leg(dev, seed=0, n_req=16, rate_hz=20.0):
     return {"value": srv.work / wall, "unit": UNIT, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
             "mean_s": st["mean_s"], "requests": len(done), "grad_requests": int(sum(r.grad for r in reqs)),
             "rate_hz": rate_hz, "wall_s": round(wall, 3), "rounds": srv.rounds,
+            "breakdown": srv.breakdown(wall),
             "peak_hbm_gb": round((torch.cuda.max_memory_allocated(dev) - base) / 2 ** 30, 3),
             "hbm_budget_gb": 180, "what": "Poisson arrivals, 48/64/96^3 grids, 2k-50k particles, horizons 5-100 env "
                                           "steps x 50 substeps, 30% gradient requests; continuous batching"}
@@ -640,60 +681,78 @@ def plain_rates(envs, dev, sample_every=8):
                     f"{len(envs[::sample_every])} sampled envs x 1 env step"}
 
 
-def cpu_baseline(envs, budget_s=12.0):
-    """FP64 C restatement (oracle/) on the host cores, the reference's schedule
-    (forward storing every substep state, then the adjoint), bounded sample."""
+def median_env(envs):
+    """The env of median particle count: the CPU sample of the batch."""
+    return sorted(envs, key=lambda e: e.n)[len(envs) // 2]
+
+
+def cpu_rollout(env, substeps):
+    """One rollout of one env on the FP64 C restatement (oracle/, OpenMP over
+    particles and cells, all host cores) in the reference's schedule: the
+    forward storing every substep's state (mpm/simulator.py:561-571), a loss
+    gradient on the final positions, then the chained substep adjoints
+    (mpm/simulator.py:573-585).  Returns the seconds it took."""
     from oracle import oracle as O
     O.set_svd_mode("reference")
-    cores = os.cpu_count()
     t0 = time.perf_counter()
-    work, done = 0, 0
-    T = 20
-    for env in envs:
-        prm = O.SimParams(grid_dim=env.grid_dim, dx=env.dx, dt=env.dt, gravity=env.gravity,
-                          ground_friction=env.ground_friction)
-        o = O.CpuMPM("oracle", prm, O.Material(env.mass, env.vol, env.mu_lam_yield),
-                     O.Bodies(env.body_tfsr, env.body_args))
-        states = [env.state()]
-        for t in range(T):
-            states.append(o.substep(states[-1], env.pose(t), env.pose(t + 1)))
-        g = {k: np.zeros_like(v, dtype=np.float64) for k, v in states[-1].items()}
-        g["x"] = np.ones_like(g["x"])
-        for t in range(T - 1, -1, -1):
-            g, _, _ = o.substep_grad(states[t], env.pose(t), env.pose(t + 1), states[t + 1]["v"], g)
-        work += env.n * T
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": work / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done} envs of the batch x {T} substeps fwd+bwd (reference schedule), FP64, OpenMP",
-            "seconds": round(dt, 2)}
+    prm = O.SimParams(grid_dim=env.grid_dim, dx=env.dx, dt=env.dt, gravity=env.gravity,
+                      ground_friction=env.ground_friction)
+    o = O.CpuMPM("oracle", prm, O.Material(env.mass, env.vol, env.mu_lam_yield),
+                 O.Bodies(env.body_tfsr, env.body_args))
+    states = [env.state()]
+    for t in range(substeps):
+        states.append(o.substep(states[-1], env.pose(t), env.pose(t + 1)))
+    g = {k: np.zeros_like(v, dtype=np.float64) for k, v in states[-1].items()}
+    g["x"] = 2.0 * (states[-1]["x"] - env.x) / env.n
+    for t in range(substeps - 1, -1, -1):
+        g, _, _ = o.substep_grad(states[t], env.pose(t), env.pose(t + 1), states[t + 1]["v"], g)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(envs):
+    """The CPU baseline beside our line: one full rollout (all env steps x
+    substeps, forward + backward) of the median env of the batch."""
+    env = median_env(envs)
+    T = SUBSTEPS * ENV_STEPS
+    dt = cpu_rollout(env, T)
+    return {"value": env.n * T / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"1 env of the batch (median size, {env.n} particles, {env.name}) x {ENV_STEPS} env steps x "
+                      f"{SUBSTEPS} substeps, fwd+bwd in the reference's schedule (every substep state stored), "
+                      f"FP64 C restatement with OpenMP", "seconds": round(dt, 2)}
 
 
 # ---------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
+    """The reference path is CUDA-only (mpm/csrc/integrator.cu); its CPU
+    implementation here is the FP64 C restatement of its kernels (oracle/),
+    run in its schedule on the host cores.  Each step is a bounded sample of
+    the batch workload: one full rollout (all env steps x substeps, forward +
+    backward) of the batch's median env.  The reference's own kernels built
+    for the host (oracle/_ref) need the reference tree to compile, which the
+    GPU hosts do not have."""
     if rank != 0:
         return
-    envs = build_batch(0, args.envs)
+    envs = build_batch(0, args.envs, args.presorted)
+    env = median_env(envs)
+    T = SUBSTEPS * ENV_STEPS
     times = []
-    cpu = None
     for k in range(args.warmup + args.steps):
-        c = cpu_baseline(envs, budget_s=6.0)
+        dt = cpu_rollout(env, T)
         if k >= args.warmup:
-            times.append(c)
-        cpu = c
-    value = float(np.mean([c["value"] for c in times])) if times else cpu["value"]
-    n_total = sum(e.n for e in envs)
+            times.append(dt)
+    sec = float(np.mean(times))
+    value = env.n * T / sec
+    sample = (f"1 env of the batch (median size, {env.n} particles, {env.name}) x {ENV_STEPS} env steps x "
+              f"{SUBSTEPS} substeps, fwd+bwd in the reference's schedule (every substep state stored)")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": n_total * SUBSTEPS * ENV_STEPS / value * 1e3,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (seeded, workloads.batch_envs)", "impl": "reference",
-           "config": {"workload": "batch: 64 envs x 64^3 grid, log-uniform 2k-30k particles, 22 capsules/env, "
-                                  "10 env steps x 50 substeps, fwd+bwd",
-                      "note": "the reference path is CUDA-only; its CPU stand-in is the FP64 C restatement "
-                              "(oracle/), timed on a bounded sample of the same envs each step"},
-           "cpu_baseline": {**cpu, "value": value},
+           "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workloads.batch_envs)",
+           "impl": "reference",
+           "config": {"workload": f"batch sample: {sample}",
+                      "note": "the reference path is CUDA-only; its CPU implementation is the FP64 C restatement "
+                              "of its kernels (oracle/), OpenMP over all host cores; each step is one full rollout "
+                              "of the sampled env, timed whole"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

@@ -18,9 +18,16 @@ from typing import Dict, Optional, Tuple
 
 import torch
 
-from .engine import SM_COUNT, BatchEngine
+from .engine import BatchEngine, sm_count
 
-CANDIDATES = [(t, c) for t in (64, 128, 256) for c in (SM_COUNT * 2, SM_COUNT * 4, SM_COUNT * 8)]
+
+def candidates_for(E: BatchEngine):
+    """Particle tile sizes x persistent grid CTAs of 2, 4 and 8 per SM of the
+    engine's device."""
+    sms = sm_count(E.device)
+    return [(t, c) for t in (64, 128, 256) for c in (sms * 2, sms * 4, sms * 8)]
+
+
 _CACHE: Dict[str, Tuple[int, int]] = {}
 CACHE_FILE = os.environ.get("DEXMPM_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache",
                                                               "dexmpm_autotune.json"))
@@ -50,10 +57,12 @@ def _save_file():
 
 
 def tune(E: BatchEngine, state: torch.Tensor, poses: torch.Tensor, reps: int = 3, use_cache: bool = True,
-         candidates=CANDIDATES, rounds: int = 3) -> Tuple[int, int]:
+         candidates=None, rounds: int = 3) -> Tuple[int, int]:
     """Time each candidate (tile_size, grid_ctas) on `state` (a state slot of
     E) with poses (>= 2 rows of [n_bodies][8]); apply and return the best."""
     key = key_for(E)
+    if candidates is None:
+        candidates = candidates_for(E)
     if use_cache:
         if not _CACHE:
             _load_file()

@@ -20,9 +20,8 @@
 // the GPU (different streams or threads, no ordering between them) race on the
 // array and give wrong results: order them on one stream.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
-
-#include <mutex>
 
 #include "../../include/dexmpm.h"
 
@@ -47,28 +46,32 @@ constexpr size_t kBytes = kCounts + 256;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
-std::mutex g_mutex;
-void *g_addr[64] = {nullptr};  // per device ordinal
-
 // Device address of the array for the current device (host code only has a
-// stand-in symbol; the address must come from the runtime).
+// stand-in symbol; the address must come from the runtime).  Looked up on
+// every call, so that it stays valid across a cudaDeviceReset, which unloads
+// and reloads the module.
 int scratch_address(void **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEXMPM_ERR_LAUNCH;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (g_addr[dev] == nullptr) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return DEXMPM_ERR_LAUNCH;
-    g_addr[dev] = p;
-  }
-  *out = g_addr[dev];
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return DEXMPM_ERR_LAUNCH;
+  *out = p;
   return DEXMPM_OK;
 }
 
+// Streaming multiprocessors of the current device (persistent grid kernels
+// launch up to four CTAs per SM).
+int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess || sms < 1)
+    return 1;
+  return sms;
+}
+
+bool positive_finite(float v) { return v > 0.f && v <= 3.0e38f; }
+
 // Writes the env descriptor, the tiles and the block->env table, and zeroes
-// the flags, list counts, ticket and (when no caller word is given) the error
-// word used by this call.
-__global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks, int32_t *caller_error) {
+// the flags, list counts and ticket used by this call.
+__global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks) {
   unsigned char *base = g_noalloc_scratch;
   int32_t *tiles = reinterpret_cast<int32_t *>(base + kTiles);
   int32_t *block_env = reinterpret_cast<int32_t *>(base + kBlockEnv);
@@ -88,7 +91,6 @@ __global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks, int32_t *
     int32_t *counts = reinterpret_cast<int32_t *>(base + kCounts);
     counts[0] = 0;  // block count of the single slot
     counts[2] = 0;  // done_counter
-    if (caller_error == nullptr) counts[3] = 0;
   }
 }
 
@@ -98,8 +100,12 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
                                       const float *vol, const float *mu_lam_yield, const float *body_shape,
                                       const float *pose, const float *next_pose, int32_t *error,
                                       dexmpm_stream_t stream) {
-  if (!env || !s || !next_s || !mass || !vol || !mu_lam_yield) return DEXMPM_ERR_ARG;
+  // the error word is required: without it an out-of-grid particle would be
+  // skipped with no sign to the caller
+  if (!env || !s || !next_s || !mass || !vol || !mu_lam_yield || !error) return DEXMPM_ERR_ARG;
   const DexEnv e = *env;
+  if (!positive_finite(e.dx) || !positive_finite(e.inv_dx) || !positive_finite(e.dt)) return DEXMPM_ERR_ARG;
+  if (fabsf(e.dx * e.inv_dx - 1.f) > 1e-4f) return DEXMPM_ERR_ARG;
   if (e.p_off != 0 || e.blk_off != 0 || e.body_off != 0 || e.n < 0 || e.n > kMaxParticles) return DEXMPM_ERR_ARG;
   if (e.gx < 8 || e.gy < 8 || e.gz < 8 || (e.gx & 3) || (e.gy & 3) || (e.gz & 3)) return DEXMPM_ERR_ARG;
   if ((long long)e.gx * e.gy * e.gz > kMaxCells) return DEXMPM_ERR_ARG;
@@ -116,7 +122,7 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   if (cudaMemsetAsync(base + kGrid0, 0, (size_t)n_blocks * 64 * 16, st) != cudaSuccess) return DEXMPM_ERR_LAUNCH;
   const int threads = 256, work = n_blocks > n_tiles ? n_blocks : n_tiles;
   const int blocks = (work + threads - 1) / threads > 0 ? (work + threads - 1) / threads : 1;
-  k_noalloc_setup<<<blocks, threads, 0, st>>>(e, n_tiles, n_blocks, error);
+  k_noalloc_setup<<<blocks, threads, 0, st>>>(e, n_tiles, n_blocks);
   if (cudaGetLastError() != cudaSuccess) return DEXMPM_ERR_LAUNCH;
 
   DexBatch b;
@@ -126,7 +132,7 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   b.n_blocks = n_blocks;
   b.n_bodies = e.n_bodies;
   b.tile_size = kTile;
-  b.grid_ctas = 152 * 4;
+  b.grid_ctas = 4 * device_sms();
   b.flags = 0;
   b.n_slots = 1;
   b.pad0 = b.pad1 = b.pad2 = 0;
@@ -145,7 +151,7 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   b.block_count = reinterpret_cast<int32_t *>(base + kCounts);
   b.done_counter = reinterpret_cast<uint32_t *>(base + kCounts + 8);
   b.body_shape = body_shape;
-  b.error = error ? error : reinterpret_cast<int32_t *>(base + kCounts + 12);
+  b.error = error;
   // one grid slot, nothing to clear afterwards (the next call re-zeroes it)
   return dexmpm_substep(&b, 0, -1, s, next_s, pose, next_pose, nullptr, stream);
 }

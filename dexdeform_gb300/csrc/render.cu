@@ -406,9 +406,15 @@ __global__ void k_smooth(const float *__restrict__ in, float *__restrict__ out, 
 
 int launched() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
 
+// Grid of a grid-stride launch over n items: at most 16 CTAs per SM of the
+// current device.
 int grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  const long long cap = 152LL * 16;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess || sms < 1)
+    sms = 1;
+  const long long cap = 16LL * sms;
   return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 

@@ -25,8 +25,14 @@ import torch
 
 from . import _native as N
 
-SM_COUNT = 152
 TAPE_PLANES = N.TAPE_PLANES
+
+
+def sm_count(device=None) -> int:
+    """Streaming multiprocessors of the device (152 on a GB300): the
+    persistent grid kernels and the autotuner's candidates are sized from it."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    return int(torch.cuda.get_device_properties(dev).multi_processor_count)
 
 
 @dataclass
@@ -172,7 +178,7 @@ class BatchEngine:
         self.done_counter = torch.zeros(1, **i32)
         self.error = torch.zeros(1, **i32)
         self.states = torch.zeros((n_slots, N.STATE_PLANES, Np), **f32)
-        self.grid_ctas = int(grid_ctas or SM_COUNT * 4)
+        self.grid_ctas = int(grid_ctas or sm_count(self.device) * 4)
         b = N.DexBatch()
         b.n_envs, b.n_particles, b.n_tiles, b.n_blocks = len(self.specs), Np, len(tiles), self.n_blocks
         b.n_bodies, b.tile_size, b.grid_ctas = self.n_bodies, self.tile_size, self.grid_ctas
@@ -460,6 +466,13 @@ class Rollout:
             run_graph(self.E, self._fwd_graphs, ("kept", k), lambda: self._forward_step_kept(k), self.use_graphs)
             self._kept_live = True
         return self._ckpt(self.S)
+
+    def state(self, k: int) -> torch.Tensor:
+        """Checkpoint k (the state at the start of env step k; k = S is the
+        final state).  Without gradients only the last two are kept."""
+        if not self.E.grad:
+            assert k >= self.S - 1, "forward-only rollouts keep the last two checkpoints"
+        return self._ckpt(k)
 
     # ------------------------------------------------------------ backward
     def _backward_step(self, k: int, recompute: bool = True):

@@ -105,8 +105,12 @@ class _Batch:
         if out is not self.gbuf[1]:
             self.gbuf[1].copy_(out)
 
-    def run(self, kind: str):
+    def run(self, kind: str) -> bool:
+        """Run the round's launch sequence; True when it was captured as a
+        new CUDA graph (first use of this membership and kind)."""
+        before = len(self.graphs)
         run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward, self.use_graphs)
+        return len(self.graphs) > before
 
 
 class Server:
@@ -136,6 +140,15 @@ class Server:
         self.max_inflight = max(1, int(max_inflight_rounds))
         self._round_reqs: List[Request] = []
         self._round_batches: list = []
+        # where the time goes: engines built and graphs captured (host
+        # seconds), and per round the device time of the state gathers, the
+        # substeps and the scatters on each stream (CUDA events, read at the
+        # end of run)
+        self.engine_builds = 0
+        self.graph_captures = 0
+        self.host_build_s = 0.0
+        self.host_capture_s = 0.0
+        self._events: list = []
 
     # ---------------------------------------------------------- admission
     def submit(self, req: Request):
@@ -163,7 +176,10 @@ class Server:
         key = (grad,) + tuple(r.rid for r in reqs)
         b = self.cache.get(key)
         if b is None:
+            t0 = time.perf_counter()
             b = _Batch(reqs, self.T, grad, self.device, self.tile_size, self.use_graphs)
+            self.engine_builds += 1
+            self.host_build_s += time.perf_counter() - t0
             self.cache[key] = b
             while len(self.cache) > self.max_cached:
                 self.cache.popitem(last=False)
@@ -172,10 +188,22 @@ class Server:
         return b
 
     # -------------------------------------------------------------- round
+    def _mark(self):
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        return ev
+
+    def _run_batch(self, b, kind):
+        t0 = time.perf_counter()
+        if b.run(kind):
+            self.graph_captures += 1
+            self.host_capture_s += time.perf_counter() - t0
+
     def _forward_round(self, reqs):
         b = self._batch(reqs, grad=False)
         self._round_batches.append(b)
         E = b.E
+        ev = [self._mark()]
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
             o = E.p_off[e]
@@ -183,7 +211,9 @@ class Server:
             t0 = r.step * self.T
             bo = E.body_off[e]
             b.poses[:, bo:bo + r.env.nb].copy_(res.poses[t0:t0 + self.T + 1])
-        b.run("fwd")
+        ev.append(self._mark())
+        self._run_batch(b, "fwd")
+        ev.append(self._mark())
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
             o = E.p_off[e]
@@ -191,11 +221,14 @@ class Server:
             if r.grad:
                 res.ckpt.append(res.state.clone())
             self.work += r.env.n * self.T
+        ev.append(self._mark())
+        self._events.append(("fwd", ev))
 
     def _backward_round(self, reqs):
         b = self._batch(reqs, grad=True)
         self._round_batches.append(b)
         E = b.E
+        ev = [self._mark()]
         b.gbuf[1].zero_()
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
@@ -210,7 +243,9 @@ class Server:
                 res.grad[0:3] = 2.0 * res.ckpt[-1][0:3] / r.env.n
             b.gbuf[1][:, o:o + r.env.n].copy_(res.grad)
         b.bgrad.zero_()
-        b.run("bwd")
+        ev.append(self._mark())
+        self._run_batch(b, "bwd")
+        ev.append(self._mark())
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
             o = E.p_off[e]
@@ -220,6 +255,8 @@ class Server:
             t0 = k * self.T
             res.bgrad[t0:t0 + self.T + 1] += b.bgrad[:, bo:bo + r.env.nb]
             self.work += r.env.n * self.T
+        ev.append(self._mark())
+        self._events.append(("bwd", ev))
 
     def step(self, now):
         """Admit what fits, run one round, retire finished requests."""
@@ -309,6 +346,29 @@ class Server:
         while inflight:
             retire(block=True)
         return self.done
+
+
+    def breakdown(self, wall_s: float) -> dict:
+        """Where the serving time went (call after run): device seconds of the
+        state gathers, the substeps and the scatters per stream, their busy
+        fraction of the wall time, and the host time spent building engines
+        and capturing graphs for new memberships."""
+        out = {"wall_s": round(wall_s, 3), "rounds": self.rounds, "engine_builds": self.engine_builds,
+               "graph_captures": self.graph_captures, "host_build_s": round(self.host_build_s, 3),
+               "host_capture_s": round(self.host_capture_s, 3)}
+        for kind in ("fwd", "bwd"):
+            g = c = sc = 0.0
+            n = 0
+            for k, ev in self._events:
+                if k != kind:
+                    continue
+                g += ev[0].elapsed_time(ev[1]) / 1e3
+                c += ev[1].elapsed_time(ev[2]) / 1e3
+                sc += ev[2].elapsed_time(ev[3]) / 1e3
+                n += 1
+            out[kind] = {"rounds": n, "gather_s": round(g, 3), "substeps_s": round(c, 3), "scatter_s": round(sc, 3),
+                         "busy_frac": round((g + c + sc) / wall_s, 3) if wall_s > 0 else None}
+        return out
 
 
 def latency_stats(done: List[Request]):

@@ -180,8 +180,10 @@ def plain_env(seed=0, steps=50, n=5000):
                     name="plain-fwd-64^3-5k")
 
 
-def batch_envs(seed=0, n_envs=64, steps=50, n_lo=2000, n_hi=30000, grid=64):
-    """Batching: log-uniform particle counts, cube or ellipsoid, yield U[30,80]."""
+def batch_envs(seed=0, n_envs=64, steps=50, n_lo=2000, n_hi=30000, grid=64, sort=True):
+    """Batching: log-uniform particle counts, cube or ellipsoid, yield U[30,80].
+    sort=False keeps each object's particles in sampling order (random
+    positions, as an object sampler hands them over)."""
     rng = np.random.default_rng(seed)
     counts = np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), n_envs)).astype(int)
     shapes = rng.integers(0, 2, n_envs)
@@ -191,11 +193,11 @@ def batch_envs(seed=0, n_envs=64, steps=50, n_lo=2000, n_hi=30000, grid=64):
         if shapes[e] == 0:
             envs.append(make_env(seed * 1000 + e + 1, int(counts[e]), "cube", grid=grid,
                                  center=(0.5, 0.15, 0.5), extent=0.2, yield_stress=float(ys[e]),
-                                 steps=steps, name=f"cube{e}"))
+                                 steps=steps, sort=sort, name=f"cube{e}"))
         else:
             envs.append(make_env(seed * 1000 + e + 1, int(counts[e]), "ellipsoid", grid=grid,
                                  center=(0.5, 0.11, 0.5), extent=(0.12, 0.06, 0.09),
-                                 yield_stress=float(ys[e]), steps=steps, name=f"ellipsoid{e}"))
+                                 yield_stress=float(ys[e]), steps=steps, sort=sort, name=f"ellipsoid{e}"))
     return envs
 
 

@@ -290,14 +290,18 @@ int dexmpm_clear_slots(const DexBatch *b, int first, int last, dexmpm_stream_t s
  *           of 4 with gx*gy*gz <= 262144 (64^3); n <= 1048576; n_bodies <= 32.
  *   s, next_s: state slots of 24 planes of env->n floats (layout above).
  *   mass, vol [n], mu_lam_yield [3][n]; body_shape, pose, next_pose [n_bodies][8].
- *   error:  nullable device int32; DEXMPM_ERR_OUT_OF_GRID is OR-ed in when a
- *           particle stencil leaves the grid (that particle is skipped).
+ *   error:  device int32, required; DEXMPM_ERR_OUT_OF_GRID is OR-ed in when
+ *           a particle stencil leaves the grid (that particle is skipped).
+ *           It is not cleared by the call.
  * Grids, active-block lists and counters live in one fixed device array of
  * this library (8.5 MB, held by every GPU that loads it until exit), shared
  * by all calls: each call clears what must start at zero, and calls that
- * overlap on the GPU race on it.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
- * Returns DEXMPM_ERR_ARG for sizes beyond the limits. */
+ * overlap on the GPU race on it.  Each call looks up the array's device
+ * address; the first call on a device also loads the library's device code
+ * there, so make that first call before any stream capture.
+ * Returns DEXMPM_ERR_ARG for sizes beyond the limits, a null pointer among
+ * the required ones, and dx, inv_dx or dt that are not positive and finite or
+ * with dx * inv_dx != 1. */
 int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *next_s, const float *mass, const float *vol,
                            const float *mu_lam_yield, const float *body_shape, const float *pose,
                            const float *next_pose, int32_t *error, dexmpm_stream_t stream);

@@ -63,6 +63,53 @@ def oracle_sim(O, env, backend="oracle"):
                     O.Bodies(env.body_tfsr, env.body_args))
 
 
+def oracle_rollout(O, env, steps, mode, state=None, storage="fp32", t0=0):
+    """FP64 oracle rollout from substep t0; returns {t: state} for t = 1 ..
+    steps (relative to t0) and the starting state under 0.  storage="fp32"
+    rounds the state to FP32 between substeps, as the reference stores it
+    (mpm/simulator.py:93-96): the dynamics amplify that rounding (e.g. at
+    contact and yield thresholds), so an FP64-state rollout measures the
+    storage format, not the kernels."""
+    O.set_svd_mode(mode)
+    try:
+        o = oracle_sim(O, env)
+        st = state if state is not None else env.state()
+        st = {k: np.asarray(v, np.float64) for k, v in st.items()}
+        out = {0: st}
+        for t in range(steps):
+            st = o.substep(st, env.pose(t0 + t), env.pose(t0 + t + 1))
+            if storage == "fp32":
+                st = {k: v.astype(np.float32).astype(np.float64) for k, v in st.items()}
+            out[t + 1] = st
+        return out
+    finally:
+        O.set_svd_mode("reference")
+
+
+def oracle_chain_adjoint(O, env, states, g_final, mode, t0=0):
+    """Chained substep adjoints of the oracle (mpm/simulator.py:573-585 in
+    reverse) over the states of oracle_rollout: the gradient of states[0] and
+    the body-pose gradients per substep boundary, (T + 1, nb, 3) and
+    (T + 1, nb, 4)."""
+    O.set_svd_mode(mode)
+    try:
+        o = oracle_sim(O, env)
+        T = len(states) - 1
+        g = {k: np.asarray(v, np.float64) for k, v in g_final.items()}
+        bp = np.zeros((T + 1, env.nb, 3))
+        br = np.zeros((T + 1, env.nb, 4))
+        for t in range(T - 1, -1, -1):
+            g, (a, b), (c, d) = o.substep_grad(states[t], env.pose(t0 + t), env.pose(t0 + t + 1),
+                                               states[t + 1]["v"], g)
+            bp[t] += a
+            br[t] += b
+            bp[t + 1] += c
+            br[t + 1] += d
+        return g, bp, br
+    finally:
+        O.set_svd_mode("reference")
+
+
 gpu = pytest.mark.gpu
 
 

@@ -1,0 +1,150 @@
+"""Parity at the sizes the benchmark runs, through the production path
+(BatchEngine + Rollout: fused kernels, kept grid slots, the SVD tape, CUDA
+graphs and, for gradients, the overlapped backward), against the FP64 oracle.
+
+* Batching configuration: the benchmark's own 64-env batch (64^3 grids,
+  log-uniform 2k-30k particles, cubes and ellipsoids, yield U[30, 80]); the
+  smallest, the median and the largest env are compared with the oracle.
+* Large single env: 128^3 grid, dx 1/128, dt 2.5e-5, 300,000 particles in two
+  stacked cubes of yield 40 and 120, 22 capsules and a palm box.
+
+Forward bar: relative L2 error <= 1e-3 on x, v, F, C after full env steps of
+50 substeps from the configurations' rest states, against the oracle with
+FP32 state storage between substeps (the reference's storage format).
+Adjoint bar: <= 1e-3 on the gradients of the initial state (x, v, F, C) and on
+the body-pose gradients, against the oracle's chained substep adjoints, from a
+perturbed state (at F = I every singular value is exactly 1 and the
+reference's SVD adjoint multiplies FP32 rounding by its clamped
+1 / (sigma_j^2 - sigma_i^2) = 1e6 factors; away from rest the gradient is
+well conditioned).
+"""
+import numpy as np
+import pytest
+
+from conftest import oracle_chain_adjoint, oracle_rollout, rel
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def cuda(native_lib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return native_lib
+
+
+def _rollout(envs, T, S):
+    from dexdeform_gb300.engine import BatchEngine, EnvSpec, Rollout
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=2 * T + 2)
+    R = Rollout(E, substeps=T, env_steps=S)
+    R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
+                               device="cuda")[:S * T + 1])
+    return E, R
+
+
+def _sampled(envs):
+    """Indices of the smallest, the median and the largest env."""
+    order = np.argsort([e.n for e in envs], kind="stable")
+    return [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
+
+
+def _seeded_gradient(E, envs, seed):
+    rng = np.random.default_rng(seed)
+    per_env = []
+    for e in envs:
+        per_env.append({"x": rng.normal(size=(e.n, 3)).astype(np.float32),
+                        "v": rng.normal(size=(e.n, 3)).astype(np.float32),
+                        "F": rng.normal(size=(e.n, 3, 3)).astype(np.float32),
+                        "C": rng.normal(size=(e.n, 3, 3)).astype(np.float32)})
+    return per_env, E.pack_state(per_env)
+
+
+def _check_adjoint(O, E, R, g0, envs, idx, st0, g_env, T, S):
+    g0 = E.unpack_state(g0)
+    bg = R.bgrad.cpu().numpy()
+    for e in idx:
+        env = envs[e]
+        states = oracle_rollout(O, env, S * T, "exact", state=st0[e])
+        want, bp, br = oracle_chain_adjoint(O, env, [states[t] for t in range(S * T + 1)], g_env[e], "exact")
+        for k in ("x", "v", "F", "C"):
+            assert rel(g0[e][k], want[k]) < 1e-3, (env.name, env.n, k, rel(g0[e][k], want[k]))
+        o = E.body_off[e]
+        got_p = bg[:, o:o + env.nb, :3]
+        got_r = bg[:, o:o + env.nb, 4:]
+        assert rel(got_p, bp) < 1e-3, (env.name, "pose position", rel(got_p, bp))
+        assert rel(got_r, br) < 1e-3, (env.name, "pose rotation", rel(got_r, br))
+
+
+def test_batch_config_full_size_forward(cuda, oracle_mod):
+    """The benchmark batch, one env step of 50 substeps (the kept last env
+    step of a gradient rollout, and the forward-only path), against the
+    oracle for the smallest, median and largest env."""
+    from dexdeform_gb300 import workloads as W
+    T = 50
+    envs = W.batch_envs(0, n_envs=64, steps=T)
+    assert sum(e.n for e in envs) > 600000
+    E, R = _rollout(envs, T, 1)
+    s0 = E.pack_state([e.state() for e in envs])
+    kept = E.unpack_state(R.forward(s0).clone())
+    plain = E.unpack_state(R.forward(s0, keep_last=False).clone())
+    assert E.error_word() == 0
+    for e in _sampled(envs):
+        env = envs[e]
+        want = oracle_rollout(oracle_mod, env, T, "exact")[T]
+        for k in ("x", "v", "F", "C"):
+            assert rel(kept[e][k], want[k]) < 1e-3, (env.name, env.n, k, rel(kept[e][k], want[k]))
+            assert rel(plain[e][k], want[k]) < 1e-3, (env.name, env.n, k, rel(plain[e][k], want[k]))
+
+
+def test_batch_config_full_size_adjoint(cuda, oracle_mod):
+    """The benchmark batch, 3 env steps x 5 substeps forward + backward with
+    the overlapped schedule (env step k - 1 recomputed on a second stream
+    while the adjoint of env step k runs), from a perturbed state with a
+    seeded gradient on every field of the final state."""
+    from dexdeform_gb300 import workloads as W
+    T, S = 5, 3
+    envs = W.batch_envs(0, n_envs=64, steps=S * T)
+    E, R = _rollout(envs, T, S)
+    assert R.overlap
+    st0 = [W.perturb_state(e, seed=7, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs]
+    g_env, g_final = _seeded_gradient(E, envs, 3)
+    R.forward(E.pack_state(st0))
+    g0 = R.backward(g_final).clone()
+    assert E.error_word() == 0
+    _check_adjoint(oracle_mod, E, R, g0, envs, _sampled(envs), st0, g_env, T, S)
+
+
+def test_large_config_forward(cuda, oracle_mod):
+    """128^3, 300,000 particles, yield 40 / 120, capsules and a palm box: two
+    env steps of 50 substeps, compared after each."""
+    from dexdeform_gb300 import workloads as W
+    T, S = 50, 2
+    env = W.large_env(0, steps=S * T)
+    assert env.n == 300000 and env.grid_dim == (128, 128, 128) and env.dt == 2.5e-5
+    assert (env.body_tfsr[:, 0] == 0).sum() == 1  # the palm box
+    E, R = _rollout([env], T, S)
+    s0 = E.pack_state([env.state()])
+    R.forward(s0)
+    got = {k: E.unpack_state(R.state(k))[0] for k in (1, 2)}
+    assert E.error_word() == 0
+    want = oracle_rollout(oracle_mod, env, S * T, "exact")
+    for k in (1, 2):
+        for f in ("x", "v", "F", "C"):
+            assert rel(got[k][f], want[k * T][f]) < 1e-3, (k * T, f, rel(got[k][f], want[k * T][f]))
+
+
+def test_large_config_adjoint(cuda, oracle_mod):
+    """The large env, 2 env steps x 5 substeps forward + backward (overlapped
+    schedule), from a perturbed state."""
+    from dexdeform_gb300 import workloads as W
+    T, S = 5, 2
+    env = W.large_env(0, steps=S * T)
+    E, R = _rollout([env], T, S)
+    assert R.overlap
+    st0 = [W.perturb_state(env, seed=8, v_scale=0.1, c_scale=1.0, f_scale=0.02)]
+    g_env, g_final = _seeded_gradient(E, [env], 4)
+    R.forward(E.pack_state(st0))
+    g0 = R.backward(g_final).clone()
+    assert E.error_word() == 0
+    _check_adjoint(oracle_mod, E, R, g0, [env], [0], st0, g_env, T, S)

@@ -5,7 +5,8 @@ pool allocator owns the GPU's memory, a real-time loop that must not block on
 an allocation): its scratch is a fixed device array inside the library.  This
 test steps one environment twice in a row with it and checks each step against
 the existing entry point (dexmpm_substep via BatchEngine), and that the second
-call changes the device's free memory by nothing.  It is collected last so that
+call changes the device's free memory by nothing; then a non-cubic grid with no
+bodies, and the argument checks.  It is collected last so that
 a failure here leaves every other test already run."""
 import ctypes
 
@@ -74,6 +75,57 @@ def test_noalloc_substep_matches_existing_entry_point_twice(native_lib):
         g = {"x": got[0:3].T, "v": got[3:6].T, "F": got[6:15].T.reshape(n, 3, 3), "C": got[15:24].T.reshape(n, 3, 3)}
         for k in ("x", "v", "F", "C"):
             assert rel(g[k], want[t][k]) < 1e-5, (t, k)
+
+    # a second call shape after the first: a non-cubic grid as large as the
+    # array allows (128 x 32 x 64 cells), no bodies and null pose pointers;
+    # its grid, flags and lists are re-zeroed for the new size
+    rng = np.random.default_rng(4)
+    n2 = 3000
+    x2 = (np.array([1.0, 0.2, 0.5]) + (rng.random((n2, 3)) - 0.5) * 0.2).astype(np.float32)
+    env2 = W.Env(grid_dim=(128, 32, 64), dx=1 / 64, dt=5e-5, gravity=(0.0, -30.0, 0.0), ground_friction=0.9,
+                 x=x2, v=(rng.normal(size=(n2, 3)) * 0.1).astype(np.float32),
+                 F=np.broadcast_to(np.eye(3, dtype=np.float32), (n2, 3, 3)).copy(),
+                 C=np.zeros((n2, 3, 3), np.float32), mass=np.full(n2, 1e-6, np.float32),
+                 vol=np.full(n2, 1e-6, np.float32), mu_lam_yield=np.tile(np.float32([2083.3, 1388.9, 50.0]), (n2, 1)),
+                 body_tfsr=np.zeros((0, 4), np.float32), body_args=np.zeros((0, 4), np.float32),
+                 poses=np.zeros((2, 0, 7), np.float32))
+    spec2 = EnvSpec.from_env(env2)
+    E2 = BatchEngine([spec2])
+    dummy = torch.zeros((1, 8), device="cuda")
+    a2, b2 = E2.pack_state([env2.state()]), E2.new_slots(1)[0]
+    E2.substep(a2, b2, dummy, dummy)
+    want2 = E2.unpack_state(b2)[0]
+    assert E2.error_word() == 0
+    desc2 = plan_layout([spec2], 128)["envs"][0]
+    st2 = env2.state()
+    h2 = np.zeros((24, n2), np.float32)
+    h2[0:3], h2[3:6] = st2["x"].T, st2["v"].T
+    h2[6:15], h2[15:24] = st2["F"].reshape(n2, 9).T, st2["C"].reshape(n2, 9).T
+    in2, out2 = torch.tensor(h2, device="cuda"), torch.zeros((24, n2), device="cuda")
+    m2, v2 = torch.tensor(env2.mass, device="cuda"), torch.tensor(env2.vol, device="cuda")
+    mly2 = torch.tensor(np.ascontiguousarray(env2.mu_lam_yield.T), device="cuda")
+    null = ctypes.c_void_p(0)
+    assert native_lib.dexmpm_substep_noalloc(ctypes.byref(desc2), N.ptr(in2), N.ptr(out2), N.ptr(m2), N.ptr(v2),
+                                             N.ptr(mly2), null, null, null, N.ptr(err), stream) == N.OK
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    got2 = out2.cpu().numpy()
+    g2 = {"x": got2[0:3].T, "v": got2[3:6].T, "F": got2[6:15].T.reshape(n2, 3, 3),
+          "C": got2[15:24].T.reshape(n2, 3, 3)}
+    for k in ("x", "v", "F", "C"):
+        assert rel(g2[k], want2[k]) < 1e-5, ("non-cubic", k)
+
+    # a null error word and invalid steps are rejected, not run
+    assert native_lib.dexmpm_substep_noalloc(ctypes.byref(desc2), N.ptr(in2), N.ptr(out2), N.ptr(m2), N.ptr(v2),
+                                             N.ptr(mly2), null, null, null, null, stream) == N.ERR_ARG
+    bad = plan_layout([spec2], 128)["envs"][0]
+    bad.dx = -bad.dx
+    assert native_lib.dexmpm_substep_noalloc(ctypes.byref(bad), N.ptr(in2), N.ptr(out2), N.ptr(m2), N.ptr(v2),
+                                             N.ptr(mly2), null, null, null, N.ptr(err), stream) == N.ERR_ARG
+    bad = plan_layout([spec2], 128)["envs"][0]
+    bad.dt = float("nan")
+    assert native_lib.dexmpm_substep_noalloc(ctypes.byref(bad), N.ptr(in2), N.ptr(out2), N.ptr(m2), N.ptr(v2),
+                                             N.ptr(mly2), null, null, null, N.ptr(err), stream) == N.ERR_ARG
 
     # sizes beyond the array are rejected, not run
     big = plan_layout([EnvSpec.from_env(W.tiny_env(0, n=64, grid=32, nb=1, steps=1))], 128)["envs"][0]
