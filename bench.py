@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--presorted", action="store_true",
                     help="particles handed over already ordered by grid cell (default: sampling order)")
     ap.add_argument("--serving-requests", type=int, default=200)
+    ap.add_argument("--sort-every", type=int, default=1,
+                    help="re-order particles by grid cell on the device every this many env steps (0: never)")
     return ap.parse_args()
 
 
@@ -195,10 +197,11 @@ def run_ours(args, rank, world, local):
     # two sets of kept grid slots: the backward recomputes env step k - 1
     # while the adjoint of env step k runs
     E = BatchEngine([EnvSpec.from_env(e) for e in envs], device=dev, grad=True, grid_slots=2 * SUBSTEPS + 2)
-    R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS, overlap=not args.no_overlap)
+    R = Rollout(E, substeps=SUBSTEPS, env_steps=ENV_STEPS, overlap=not args.no_overlap, sort_every=args.sort_every)
     poses_h = E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs])
     R.poses.copy_(torch.from_numpy(poses_h))
     s0 = E.pack_state([e.state() for e in envs])
+    R.sort_initial(s0)  # the launch shape is tuned on the order the rollout runs in
     tgt = E.pack_state([{"x": t, "v": np.zeros_like(t), "F": np.zeros((len(t), 3, 3), np.float32),
                          "C": np.zeros((len(t), 3, 3), np.float32)} for t in targets_for(envs)])
     counts = torch.zeros(E.n_particles, device=dev)
@@ -206,7 +209,7 @@ def run_ours(args, rank, world, local):
         counts[E.p_off[e]:E.p_off[e] + env.n] = 1.0 / env.n
     g_final = torch.zeros_like(s0)
     from dexdeform_gb300.autotune import tune
-    tuned = (E.tile_size, E.grid_ctas) if args.no_tune else tune(E, s0, R.poses[:4], use_cache=False)
+    tuned = (E.tile_size, E.grid_ctas) if args.no_tune else tune(E, R.stored(0), R.poses[:4], use_cache=False)
 
     def loss_grad(final):
         # L = sum_e mean_p |x - target|^2 ; dL/dx = 2 (x - target) / n_e
@@ -300,6 +303,7 @@ def run_ours(args, rank, world, local):
     overlapped = R.overlap
 
     plain = None if (args.no_plain or rank != 0) else plain_rates(envs, dev)
+    dropin = None if (args.no_plain or rank != 0) else plain_rates(envs, dev, backend="batched")
     cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs)
     del R, E
     serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank, n_req=args.serving_requests)
@@ -319,7 +323,9 @@ def run_ours(args, rank, world, local):
                        "dx": 1 / 64, "dt": 5e-5, "parallelism": f"replicas x{world}",
                        "launch_shape": {"tile_size": tuned[0], "grid_ctas": tuned[1],
                                         "source": "default" if args.no_tune else "autotune"},
-                       "particle_order": "presorted by grid cell" if args.presorted else "sampling order",
+                       "particle_order": ("presorted by grid cell" if args.presorted else "sampling order") +
+                                         (f"; device sort every {args.sort_every} env step(s), inside the timed "
+                                          "region" if args.sort_every else "; no device sort"),
                        "backward": ("recompute of env step k-1 on a second stream during the adjoint of env step k"
                                     if overlapped else "recompute, then adjoint, per env step"),
                        "l2": "inputs larger than L2 (per-step state traffic ~4 GB >> 129 MB L2)"},
@@ -332,6 +338,8 @@ def run_ours(args, rank, world, local):
             "kernels_us": {k: round(v, 2) for k, v in kt.items()},
             "error_word": err,
         }
+        if dropin is not None:
+            out["simulator_dropin"] = dropin
         if plain is not None:
             out["plain"] = plain
             out["batched_vs_plain"] = {"fwd": fwd_value / plain["fwd"], "fwd_bwd": value / plain["fwd_bwd"]}
@@ -367,6 +375,16 @@ def kernel_times(E, R, s0, g_final):
         acc.setdefault(name, []).append((a, b))
 
     ring, ck = R.ring, R.ckpt
+    # the particle sort of an env-step boundary (sort + state permute, then
+    # the material), and the gradient's way back through it, as a rollout
+    # runs them once per env step
+    if R._sorted:
+        perm = E.identity_perm(1)[0]
+        mat = torch.empty_like(E.mat)
+        timed("sort", lambda: E.sort(R.src, ring[1], perm))
+        timed("permute_material", lambda: E.permute(perm, E.mat, mat))
+        timed("permute_grad", lambda: E.permute(perm, ring[1], ring[2], inverse=True))
+    E.use_material(R.material(0))
 
     def pass_(sts, kept):
         """One env step of the fused sequence: P2G, grid update, then T - 1 x
@@ -427,6 +445,10 @@ def kernel_times(E, R, s0, g_final):
 # Algorithmic bytes per particle (N) and per cell of the active blocks (A)
 # for each kernel: particle state read/written once, grid float4 cells once.
 ALG_BYTES = {
+    "sort": (236, 0),          # x read, key + rank written and read, perm written and segment-sorted; 24 planes
+                               # gathered (96 B read, 96 B written, perm read)
+    "permute_material": (44, 0),  # 5 material planes gathered, perm read
+    "permute_grad": (196, 0),  # 24 gradient planes scattered back, perm read
     "p2g": (152, 16),          # x v F C + m vol mu lam yield read, F' written; m,mv scattered
     "p2g_tape": (284, 16),     # as p2g, plus the 33-plane tape written (recompute of the backward)
     "g2p2g": (164, 32),        # x, F + material read, x v C and F' written; v_out gathered, m,mv scattered
@@ -450,11 +472,12 @@ NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 
 # launch, from an ncu capture on the same batch (profiles/l2_atomics_batch64.md):
 # (lts__t_requests_op_red.sum, lts__t_sectors_op_red.sum,
 #  lts__d_atomic_input_cycles_active.avg.pct_of_peak_sustained_elapsed)
-NCU_L2_RED = {}
+NCU_L2_RED = {"g2p2g": (3212980, 5181759, 10.93), "g2p2g_tape": (3215606, 5185041, 10.06),
+              "p2g2g_grad": (3208150, 5169492, 7.56)}
 
 # kernel function of each timed launch variant (the forward pass and the
 # recompute launch the same function, the recompute with the tape written)
-FUNCTION = {"p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape": "k_g2p2g",
+FUNCTION = {"sort": "dexmpm_sort", "permute_material": "k_permute", "permute_grad": "k_permute", "p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape": "k_g2p2g",
             "grid_op": "k_grid_op", "grid_op_keep": "k_grid_op", "g2p": "k_g2p", "g2p_grad": "k_g2p_grad",
             "grid_op_grad": "k_grid_op_grad", "p2g_grad": "k_p2g_grad", "p2g2g_grad": "k_p2g2g_grad"}
 
@@ -462,7 +485,7 @@ FUNCTION = {"p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape
 # launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
 def launches_per_substep(T):
-    return {"p2g": 1 / T, "p2g_tape": 1 / T, "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1,
+    return {"sort": 1 / T, "permute_material": 1 / T, "permute_grad": 1 / T, "p2g": 1 / T, "p2g_tape": 1 / T, "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1,
             "grid_op_keep": 1, "g2p": 2 / T, "g2p_grad": 1 / T, "grid_op_grad": 1, "p2g_grad": 1 / T,
             "p2g2g_grad": 1 - 1 / T}
 
@@ -552,7 +575,7 @@ def large_env_leg(dev, substeps=100, env_steps=10):
     import torch
     from dexdeform_gb300 import workloads as W
     from dexdeform_gb300.engine import BatchEngine, EnvSpec, Rollout
-    env = W.large_env(0, steps=substeps * env_steps)
+    env = W.large_env(0, steps=substeps * env_steps, sort=False)
     base = torch.cuda.memory_allocated(dev)
     torch.cuda.reset_peak_memory_stats(dev)
     E = BatchEngine([EnvSpec.from_env(env)], device=dev, grad=True, grid_slots=2 * substeps + 2)
@@ -640,10 +663,12 @@ def render_leg(dev, cpu=True):
     return out
 
 
-def plain_rates(envs, dev, sample_every=8):
-    """Plain per-env sequential path: the reference's schedule (memsets + per-kernel
-    launches, full per-substep state storage) on the reference-compatible
-    launchers, one env at a time, for a sample of the batch's envs."""
+def plain_rates(envs, dev, sample_every=8, backend="reference"):
+    """Plain per-env sequential path: the reference's schedule (per-substep
+    calls, full per-substep state storage) through the drop-in MPMSimulator,
+    one env at a time, for a sample of the batch's envs.  backend
+    "reference": the reference-compatible launchers (memsets + four kernels
+    per substep); "batched": the same schedule on the batched kernels."""
     import torch
     from dexdeform_gb300.simulator import MPMSimulator
     T = SUBSTEPS
@@ -651,7 +676,7 @@ def plain_rates(envs, dev, sample_every=8):
     work = 0
     for env in envs[::sample_every]:
         sim = MPMSimulator(env.nb, n_particles=env.n, dx=env.dx, dt=env.dt, grid_size=(1, 1, 1), max_steps=T + 1,
-                           substeps=T, gravity=(0, -1, 0), ground_friction=env.ground_friction)
+                           substeps=T, gravity=(0, -1, 0), ground_friction=env.ground_friction, backend=backend)
         sim.init_particles(env.vol.astype(np.float64), env.mass.astype(np.float64), env.mu_lam_yield.astype(np.float64))
         sim.init_bodies(env.body_tfsr[:, 0], env.body_tfsr[:, 2], env.body_tfsr[:, 1], env.body_tfsr[:, 3],
                         env.body_args, None)
@@ -677,7 +702,7 @@ def plain_rates(envs, dev, sample_every=8):
         work += env.n * T
         del sim
     return {"fwd": work / fwd_t, "fwd_bwd": work / bwd_t, "unit": UNIT,
-            "what": f"reference schedule on the reference-compatible launchers, one env at a time, "
+            "what": f"reference schedule through MPMSimulator (backend {backend!r}), one env at a time, "
                     f"{len(envs[::sample_every])} sampled envs x 1 env step"}
 
 

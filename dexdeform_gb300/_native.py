@@ -42,6 +42,19 @@ class DexBatch(ctypes.Structure):
                 ("body_shape", c_void_p), ("error", c_void_p)]
 
 
+class DexSortWork(ctypes.Structure):
+    _fields_ = [("cell_count", c_void_p), ("cell_start", c_void_p), ("block_total", c_void_p),
+                ("block_base", c_void_p), ("block_flag", c_void_p), ("block_list", c_void_p), ("rank", c_void_p),
+                ("key", c_void_p), ("partial", c_void_p), ("counters", c_void_p)]
+
+
+SORT_CHUNK = 4096  # DEXMPM_SORT_CHUNK
+
+
+def sort_partials(n_blocks: int) -> int:
+    return (n_blocks + SORT_CHUNK - 1) // SORT_CHUNK
+
+
 assert ctypes.sizeof(DexEnv) == 64
 
 P = c_void_p
@@ -74,6 +87,8 @@ _BATCH_SIGS = {
     "dexmpm_p2g_g2p_grad": [POINTER(DexBatch), c_int, c_int, P, P, P, P, P, P, P],
     "dexmpm_get_error": [POINTER(DexBatch), POINTER(c_int32), P],
     "dexmpm_substep_noalloc": [POINTER(DexEnv), P, P, P, P, P, P, P, P, P, P],
+    "dexmpm_sort": [POINTER(DexBatch), POINTER(DexSortWork), P, P, P, P],
+    "dexmpm_permute": [P, P, P, c_int, c_int, c_int, P],
     "dexmpm_abi_get_error": [POINTER(c_int32)],
 }
 

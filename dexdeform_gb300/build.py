@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libdexmpm.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["batched.cu", "ref_abi.cu", "noalloc.cu", "render.cu"]
+SOURCES = ["batched.cu", "sort.cu", "ref_abi.cu", "noalloc.cu", "render.cu"]
 # the renderer keeps the reference's unfused float arithmetic (its images are
 # compared pixel by pixel with the reference's code run on the host)
 SOURCE_FLAGS = {"render.cu": ["-fmad=false"]}

@@ -26,6 +26,7 @@ import torch
 from . import _native as N
 
 TAPE_PLANES = N.TAPE_PLANES
+MATERIAL_PLANES = 5  # mass, vol, mu, lambda, yield stress
 
 
 def sm_count(device=None) -> int:
@@ -120,11 +121,13 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
 class BatchEngine:
     def __init__(self, specs: Sequence[EnvSpec], device="cuda", tile_size: int = 128,
                  grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False,
-                 capsule_grad: str = "reference", grid_slots: int = 2):
+                 capsule_grad: str = "reference", grid_slots: int = 2, stride: int = 0):
         """grid_slots: 2 for forward use; 2 + T lets Rollout / DiffSim keep the
         grids of a recomputed env step of T substeps for the adjoint.
         capsule_grad: "reference" drops the capsule-normal term of the body
-        pose gradient as the reference does; "exact" keeps it."""
+        pose gradient as the reference does; "exact" keeps it.  stride: at
+        least this many entries per state plane (the planes of a caller's
+        storage sized for more particles than the envs hold now)."""
         N.require_cuda()
         self.lib = N.load()
         self.device = torch.device(device)
@@ -136,7 +139,7 @@ class BatchEngine:
             assert all(g % 4 == 0 and g >= 8 for g in s.grid_dim), "grid dims must be multiples of 4"
             if s.nb > N.MAX_BODIES:
                 raise N.DexError(f"{s.nb} bodies > {N.MAX_BODIES} per env")
-        n_real = sum(s.n for s in self.specs)
+        n_real = max(sum(s.n for s in self.specs), int(stride))
         self.n_particles = max(32, ((n_real + 31) // 32) * 32)
         L = plan_layout(self.specs, self.tile_size)
         self.p_off, self.blk_off, self.body_off = L["p_off"], L["blk_off"], L["body_off"]
@@ -150,21 +153,19 @@ class BatchEngine:
                                     **i32)
         self.block_env_t = torch.tensor(np.asarray(block_env, np.int32), **i32)
         Np = self.n_particles
-        mass = np.zeros(Np, np.float32)
-        vol = np.zeros(Np, np.float32)
-        mly = np.zeros((3, Np), np.float32)
+        # material planes: mass, vol, mu, lambda, yield stress
+        mat = np.zeros((MATERIAL_PLANES, Np), np.float32)
         shapes = np.zeros((max(self.n_bodies, 1), 8), np.float32)
         for e, s in enumerate(self.specs):
             o = self.p_off[e]
-            mass[o:o + s.n] = s.mass
-            vol[o:o + s.n] = s.vol
-            mly[:, o:o + s.n] = np.asarray(s.mu_lam_yield, np.float32).T
+            mat[0, o:o + s.n] = s.mass
+            mat[1, o:o + s.n] = s.vol
+            mat[2:5, o:o + s.n] = np.asarray(s.mu_lam_yield, np.float32).T
             if s.nb:
                 shapes[self.body_off[e]:self.body_off[e] + s.nb, :4] = s.body_tfsr
                 shapes[self.body_off[e]:self.body_off[e] + s.nb, 4:] = s.body_args
-        self.mass = torch.tensor(mass, **f32)
-        self.vol = torch.tensor(vol, **f32)
-        self.mly = torch.tensor(mly, **f32)
+        self.mat = torch.tensor(mat, **f32)
+        self.mass, self.vol, self.mly = self.mat[0], self.mat[1], self.mat[2:5]
         self.body_shape = torch.tensor(shapes, **f32)
         cells = self.n_blocks * 64
         self.n_grid_slots = K = max(2, int(grid_slots))
@@ -197,7 +198,67 @@ class BatchEngine:
         self._bp = ctypes.byref(b)
         self.fslot = 0          # grid slot of the next forward substep (0 or 1)
         self.launches = 0
+        self._sortw = None      # scratch of the particle sort, allocated on first use
         N.check(self.lib.dexmpm_reset(self._bp, N.stream_ptr()), "dexmpm_reset")
+
+    # ------------------------------------------------------------ material
+    def use_material(self, mat: Optional[torch.Tensor] = None):
+        """Material planes (MATERIAL_PLANES, n_particles) the next launches
+        read: mass, vol, mu, lambda, yield stress in the particle order of the
+        states they step (None: the engine's own, in the specs' order).  The
+        pointers are copied into each launch, so CUDA graphs captured after
+        this call keep them."""
+        m = self.mat if mat is None else mat
+        assert m.shape == (MATERIAL_PLANES, self.n_particles) and m.is_contiguous()
+        b = self.batch
+        b.mass, b.vol, b.mu_lam_yield = m[0].data_ptr(), m[1].data_ptr(), m[2].data_ptr()
+
+    # ------------------------------------------------------ particle order
+    def identity_perm(self, n: int = 1) -> torch.Tensor:
+        """n permutations of the engine's particles, each the identity."""
+        return torch.arange(self.n_particles, dtype=torch.int32, device=self.device).repeat(n, 1)
+
+    def _sort_work(self):
+        if self._sortw is None:
+            dev, i32 = self.device, torch.int32
+            cells = self.n_blocks * 64
+            t = {"cell_count": torch.zeros(cells, dtype=i32, device=dev),
+                 "cell_start": torch.zeros(cells, dtype=i32, device=dev),
+                 "block_total": torch.zeros(self.n_blocks, dtype=i32, device=dev),
+                 "block_base": torch.zeros(self.n_blocks, dtype=i32, device=dev),
+                 "block_flag": torch.zeros(self.n_blocks, dtype=i32, device=dev),
+                 "block_list": torch.zeros(self.n_blocks, dtype=i32, device=dev),
+                 "rank": torch.zeros(self.n_particles, dtype=i32, device=dev),
+                 "key": torch.zeros(self.n_particles, dtype=i32, device=dev),
+                 "partial": torch.zeros(N.sort_partials(self.n_blocks), dtype=i32, device=dev),
+                 "counters": torch.zeros(4, dtype=i32, device=dev)}
+            w = N.DexSortWork()
+            for k, v in t.items():
+                setattr(w, k, v.data_ptr())
+            self._sortw = (t, w, ctypes.byref(w))
+        return self._sortw[2]
+
+    def sort(self, s: torch.Tensor, sorted_s: torch.Tensor, perm: torch.Tensor):
+        """Order every env's particles of state slot s by grid block, cell and
+        previous index: perm[i] = index in s of the particle that goes to i,
+        sorted_s = s gathered by perm.  perm's entries beyond the envs'
+        particles are left as they are (start from identity_perm)."""
+        assert perm.dtype == torch.int32 and perm.numel() == self.n_particles
+        N.check(self.lib.dexmpm_sort(self._bp, self._sort_work(), N.ptr(s), N.ptr(sorted_s), N.ptr(perm),
+                                     N.stream_ptr()), "dexmpm_sort")
+        self.launches += 7
+
+    def permute(self, perm: torch.Tensor, src: torch.Tensor, dst: torch.Tensor, inverse: bool = False):
+        """dst = src gathered by perm (dst[.., i] = src[.., perm[i]]), or with
+        inverse scattered back (dst[.., perm[i]] = src[.., i]); planes of
+        n_particles 32-bit values (floats or int32)."""
+        n = self.n_particles
+        assert src.shape[-1] == n and dst.shape == src.shape and src.is_contiguous() and dst.is_contiguous()
+        assert src.element_size() == 4 and dst.element_size() == 4
+        planes = src.numel() // n
+        N.check(self.lib.dexmpm_permute(N.ptr(perm), N.ptr(src), N.ptr(dst), n, planes, int(inverse),
+                                        N.stream_ptr()), "dexmpm_permute")
+        self.launches += 1
 
     # ----------------------------------------------------------- state I/O
     def new_slots(self, n: int) -> torch.Tensor:
@@ -396,10 +457,22 @@ class Rollout:
     slots (and `overlap`), the backward keeps two sets of slots, tapes and
     state rings and recomputes env step k - 1 on a second stream while the
     adjoint of env step k runs.  Each env step's forward, recompute and
-    adjoint are captured as CUDA graphs on first use and replayed afterwards."""
+    adjoint are captured as CUDA graphs on first use and replayed afterwards.
+
+    Particle order (`sort_every` > 0): at the start of every sort_every-th
+    env step the particles are re-ordered on the device by grid cell
+    (BatchEngine.sort) -- the first from the caller's order -- so that the
+    scatters pre-reduce well whatever order the caller hands over and however
+    the particles drift.  Checkpoint k is stored in env step k's order with
+    that order's material; the end state of an env step followed by a sort
+    goes to a scratch slot first.  The backward maps the gradient of each
+    sorted checkpoint back through the permutation.  forward() takes and
+    returns states in the caller's order, backward() takes and returns
+    gradients in it; `order(k)` gives the caller's index of every particle of
+    checkpoint k."""
 
     def __init__(self, engine: BatchEngine, substeps: int, env_steps: int, use_graphs: bool = True,
-                 overlap: bool = True):
+                 overlap: bool = True, sort_every: int = 1):
         self.E = engine
         self.T, self.S = int(substeps), int(env_steps)
         self.use_graphs = use_graphs
@@ -408,6 +481,7 @@ class Rollout:
         self.poses = torch.zeros((self.S * self.T + 1, nb, 8), dtype=torch.float32, device=dev)
         self.keep_grids = engine.n_grid_slots >= self.T + 2
         self.overlap = bool(overlap) and engine.grad and engine.n_grid_slots >= 2 * self.T + 2
+        self.sort_every = max(0, int(sort_every))
         self.tape = None
         if engine.grad:
             self.ckpt = engine.new_slots(self.S + 1)
@@ -426,35 +500,100 @@ class Rollout:
             self._side = torch.cuda.Stream(device=dev)
         self._fwd_graphs, self._bwd_graphs = {}, {}
         self._kept_live = False  # slots 2..T+1 and the tape hold the last env step's forward
+        # particle order: sorted boundaries, their permutations, the material
+        # and the caller's indices in each sorted order
+        self._sorted = [k for k in range(self.S) if self.sort_every and k % self.sort_every == 0]
+        if self._sorted:
+            m = len(self._sorted)
+            self.src = engine.new_slots(1)[0]    # the caller's initial state
+            self.tail = engine.new_slots(1)[0]   # end of an env step that a sort follows
+            self.out = engine.new_slots(1)[0]    # the final state in the caller's order
+            self.perm = engine.identity_perm(m)
+            self.orders = engine.identity_perm(m)
+            self.mats = torch.zeros((m,) + tuple(engine.mat.shape), dtype=torch.float32, device=dev)
+
+    # ------------------------------------------------------- particle order
+    def _sidx(self, k: int) -> int:
+        """Index (into perm, orders, mats) of the last sorted boundary <= k, or -1."""
+        j = -1
+        for i, b in enumerate(self._sorted):
+            if b <= k:
+                j = i
+        return j
+
+    def material(self, k: int) -> torch.Tensor:
+        """Material planes in the particle order of env step k."""
+        j = self._sidx(k)
+        return self.E.mat if j < 0 else self.mats[j]
+
+    def order(self, k: int) -> Optional[torch.Tensor]:
+        """Caller's index of each particle of checkpoint k (k = S: the final
+        state); None when the order is the caller's."""
+        j = self._sidx(min(k, self.S - 1))
+        return None if j < 0 else self.orders[j]
+
+    def _sort_boundary(self, k: int, pre: torch.Tensor):
+        """Sorted boundary k: checkpoint k = pre (the end of env step k - 1,
+        or the caller's state) in the new order, with its permutation, the
+        material in that order and the caller's indices."""
+        E, j = self.E, self._sorted.index(k)
+        E.sort(pre, self._ckpt(k), self.perm[j])
+        E.permute(self.perm[j], self.E.mat if j == 0 else self.mats[j - 1], self.mats[j])
+        if j == 0:
+            self.orders[0].copy_(self.perm[0])
+        else:
+            E.permute(self.perm[j], self.orders[j - 1], self.orders[j])
+
+    def _end(self, k: int) -> torch.Tensor:
+        """Where the forward of env step k leaves its final state."""
+        return self.tail if (k + 1 < self.S and (k + 1) in self._sorted) else self._ckpt(k + 1)
 
     # ------------------------------------------------------------- forward
     def _ckpt(self, k):
         return self.ckpt[k] if self.E.grad else self.ckpt[k % 2]
 
     def _forward_step(self, k: int):
-        """Env step k: ckpt[k] -> ckpt[k+1] through T substeps (two ring
+        """Env step k: (sort) ckpt[k] -> its end through T substeps (two ring
         buffers for the intermediate states)."""
         T = self.T
-        sts = [self._ckpt(k)] + [self.ring[t % 2] for t in range(1, T)] + [self._ckpt(k + 1)]
+        if k in self._sorted:
+            self._sort_boundary(k, self.src if k == 0 else self.tail)
+        self.E.use_material(self.material(k))
+        sts = [self._ckpt(k)] + [self.ring[t % 2] for t in range(1, T)] + [self._end(k)]
         self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1])
 
     def _forward_step_kept(self, k: int):
-        """Env step k as the backward recomputes it: states into the ring,
-        grids kept in slots 2..T+1, the tape written; result in ckpt[k+1]."""
+        """Env step k (the last) as the backward recomputes it: states into
+        the ring, grids kept in slots 2..T+1, the tape written; result in
+        ckpt[k+1]."""
         T = self.T
+        if k in self._sorted:
+            self._sort_boundary(k, self.src if k == 0 else self.tail)
+        self.E.use_material(self.material(k))
         sts = [self.ckpt[k]] + [self.ring[t] for t in range(1, T)] + [self.ckpt[k + 1]]
         self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=self.tape)
 
     def forward_step(self, k: int):
         self._run(self._fwd_graphs, k, self._forward_step)
 
-    def forward(self, state0: Optional[torch.Tensor] = None, keep_last: bool = True):
-        """Run the S env steps from ckpt[0] (or state0).  keep_last (gradient
-        engines with kept grids): run the last env step as the backward would
-        recompute it, for a backward that follows; pass False for forward-only
-        use."""
-        if state0 is not None:
+    def sort_initial(self, state0: torch.Tensor):
+        """Checkpoint 0 and its material from the caller's state0 (eager),
+        e.g. to tune launch shapes on the order the rollout will run."""
+        if 0 in self._sorted:
+            self.src.copy_(state0)
+            self._sort_boundary(0, self.src)
+        else:
             self._ckpt(0).copy_(state0)
+        self.E.use_material(self.material(0))
+
+    def forward(self, state0: Optional[torch.Tensor] = None, keep_last: bool = True):
+        """Run the S env steps from state0 (the caller's order; None: the
+        state of the previous call).  keep_last (gradient engines with kept
+        grids): run the last env step as the backward would recompute it, for
+        a backward that follows; pass False for forward-only use.  Returns
+        the final state in the caller's order."""
+        if state0 is not None:
+            (self.src if 0 in self._sorted else self._ckpt(0)).copy_(state0)
         keep = keep_last and self.E.grad and self.keep_grids and self.S > 0
         if self._kept_live:
             self.E.clear_slots(2, 2 + self.T)  # a kept forward whose backward was not taken
@@ -465,23 +604,50 @@ class Rollout:
             k = self.S - 1
             run_graph(self.E, self._fwd_graphs, ("kept", k), lambda: self._forward_step_kept(k), self.use_graphs)
             self._kept_live = True
-        return self._ckpt(self.S)
+        return self._to_caller(self._ckpt(self.S), self.S, self.out if self._sorted else None)
+
+    def _to_caller(self, st: torch.Tensor, k: int, out: Optional[torch.Tensor]):
+        o = self.order(k)
+        if o is None:
+            return st
+        self.E.permute(o, st, out, inverse=True)
+        return out
+
+    def stored(self, k: int) -> torch.Tensor:
+        """Checkpoint k as stored: in env step k's particle order."""
+        return self._ckpt(k)
 
     def state(self, k: int) -> torch.Tensor:
         """Checkpoint k (the state at the start of env step k; k = S is the
-        final state).  Without gradients only the last two are kept."""
+        final state) in the caller's order.  Without gradients only the last
+        two are kept."""
         if not self.E.grad:
             assert k >= self.S - 1, "forward-only rollouts keep the last two checkpoints"
-        return self._ckpt(k)
+        st = self._ckpt(k)
+        return self._to_caller(st, k, torch.empty_like(st))
 
     # ------------------------------------------------------------ backward
+    def _end_for_adjoint(self, k: int, ring) -> torch.Tensor:
+        """The end state of env step k in its own order: the checkpoint after
+        it, unless a sort followed (then the recompute left it in ring[T])."""
+        return ring[self.T] if (k + 1 < self.S and (k + 1) in self._sorted) else self.ckpt[k + 1]
+
+    def _unsort_grad(self, k: int):
+        """Gradient of checkpoint k (gbuf[1]) -> gradient of what was sorted
+        into it (the end of env step k - 1, or the caller's state)."""
+        if k in self._sorted:
+            j = self._sorted.index(k)
+            self.E.permute(self.perm[j], self.gbuf[1], self.gbuf[0], inverse=True)
+            self.gbuf[1].copy_(self.gbuf[0])
+
     def _backward_step(self, k: int, recompute: bool = True):
-        """Gradient of ckpt[k] from the gradient of ckpt[k+1] (in gbuf[1]):
-        recompute the T states of env step k into the ring (keeping each
-        substep's grid slot when there are enough slots) unless the forward
-        kept them, then run the adjoint substeps in reverse.  Result in
-        gbuf[1]."""
+        """Gradient of ckpt[k] from the gradient of the end of env step k (in
+        gbuf[1]): recompute the T states of env step k into the ring (keeping
+        each substep's grid slot when there are enough slots) unless the
+        forward kept them, then run the adjoint substeps in reverse; then back
+        through the sort of boundary k.  Result in gbuf[1]."""
         T, E = self.T, self.E
+        E.use_material(self.material(k))
         if recompute and self.keep_grids:
             sts = [self.ckpt[k]] + [self.ring[t] for t in range(1, T + 1)]
             E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=self.tape)
@@ -491,23 +657,26 @@ class Rollout:
                 t = k * T + s
                 E.substep(src, self.ring[s + 1], self.poses[t], self.poses[t + 1])
                 src = self.ring[s + 1]
+        end = self._end_for_adjoint(k, self.ring)
         if self.keep_grids:
-            sts = [self.ckpt[k]] + [self.ring[s] for s in range(1, T)] + [self.ckpt[k + 1]]
+            sts = [self.ckpt[k]] + [self.ring[s] for s in range(1, T)] + [end]
             out = E.run_adjoint(sts, self.gbuf[1], self.gbuf[0], self.poses[k * T:k * T + T + 1],
                                 self.bgrad[k * T:k * T + T + 1], tapes=self.tape)
             if out is not self.gbuf[1]:
                 self.gbuf[1].copy_(out)
+            self._unsort_grad(k)
             return
         g_next, g = self.gbuf[1], self.gbuf[0]
         for s in range(T - 1, -1, -1):
             t = k * T + s
             cur = self.ckpt[k] if s == 0 else self.ring[s]
-            nxt = self.ckpt[k + 1] if s == T - 1 else self.ring[s + 1]
+            nxt = end if s == T - 1 else self.ring[s + 1]
             E.substep_grad(cur, nxt, g_next, g, self.poses[t], self.poses[t + 1], self.bgrad[t],
                            self.bgrad[t + 1], tape=self._tape(s))
             g_next, g = g, g_next
         if T % 2 == 1:
             self.gbuf[1].copy_(self.gbuf[0])
+        self._unsort_grad(k)
 
     def _tape(self, s):
         return None if self.tape is None else self.tape[s]
@@ -524,12 +693,19 @@ class Rollout:
             self._run(self._bwd_graphs, k, self._backward_step)
 
     def backward(self, g_final: torch.Tensor, on_boundary=None):
-        """Back-propagate g_final (gradient of the last checkpoint).
-        on_boundary(k, g) may add loss gradients of checkpoint k in place.
-        Returns the gradient of ckpt[0]; body-pose gradients land in bgrad."""
+        """Back-propagate g_final (gradient of the final state, caller's
+        order).  on_boundary(k, g) may add loss gradients of the state at
+        boundary k in place; g is in the particle order of env step k - 1
+        (order(k - 1) maps it to the caller's; the caller's order for k = 0).
+        Returns the gradient of the initial state in the caller's order;
+        body-pose gradients land in bgrad."""
         assert self.E.grad
         self.bgrad.zero_()
-        self.gbuf[1].copy_(g_final)
+        o = self.order(self.S)
+        if o is None:
+            self.gbuf[1].copy_(g_final)
+        else:
+            self.E.permute(o, g_final.contiguous(), self.gbuf[1])
         if self.overlap and self.S > 1:
             self._backward_overlapped(on_boundary)
             return self.gbuf[1]
@@ -550,19 +726,23 @@ class Rollout:
         set's ring, grids kept, tape written)."""
         T = self.T
         base, ring, tape = self._set_of(k)
+        self.E.use_material(self.material(k))
         sts = [self.ckpt[k]] + [ring[t] for t in range(1, T + 1)]
         self.E.run_substeps(sts, self.poses[k * T:k * T + T + 1], kept=True, tapes=tape, slot_base=base)
 
     def _adjoint(self, k: int):
-        """Adjoint of env step k from its slot set; gradient of ckpt[k+1] in
-        gbuf[1] in, gradient of ckpt[k] in gbuf[1] out."""
+        """Adjoint of env step k from its slot set; gradient of the end of
+        env step k in gbuf[1] in, gradient of what precedes ckpt[k] (back
+        through the sort of boundary k) in gbuf[1] out."""
         T = self.T
         base, ring, tape = self._set_of(k)
-        sts = [self.ckpt[k]] + [ring[t] for t in range(1, T)] + [self.ckpt[k + 1]]
+        self.E.use_material(self.material(k))
+        sts = [self.ckpt[k]] + [ring[t] for t in range(1, T)] + [self._end_for_adjoint(k, ring)]
         out = self.E.run_adjoint(sts, self.gbuf[1], self.gbuf[0], self.poses[k * T:k * T + T + 1],
                                  self.bgrad[k * T:k * T + T + 1], tapes=tape, slot_base=base)
         if out is not self.gbuf[1]:
             self.gbuf[1].copy_(out)
+        self._unsort_grad(k)
 
     def _backward_overlapped(self, on_boundary):
         """Env steps S-1 .. 0: the adjoint of env step k on the current stream

@@ -2,16 +2,27 @@
 TempState, rigid_body_motion) on libdexmpm.so.
 
 Same constructor arguments, state tuples, per-substep ``states`` list and
-substep / substep_grad schedule (mpm/simulator.py:561-585), backed by the
-reference-compatible launchers of include/dexmpm.h (AoS arrays, dense grid) and
-by torch device tensors instead of the reference's cudaMalloc'd ``array``
-objects.  Differences: no yacs config (keyword arguments, ``cfg`` accepted and
-ignored except for ``gravity`` / ``ground_friction`` attributes), and
-device-side pose copies (``set_pose`` accepts device tensors without a host
-round trip).
+substep / substep_grad schedule (mpm/simulator.py:561-585).  Two backends:
+
+* ``"batched"`` (default): the states live in the batched engine's layout
+  (24 SoA planes per state, dexdeform_gb300.engine) and every substep runs the
+  batched kernels -- fused SVD/stress/P2G with warp pre-reduction, the
+  block-culled grid update, coalesced G2P; ``step`` fuses each G2P with the
+  next P2G.  ``states[i].x`` etc. keep the interface of mpm/types.py's
+  ``array`` (upload, download, zero, ``.t``) as strided views of the planes,
+  so reads and writes convert between the caller's (n, 3) / (n, 3, 3) arrays
+  and the planes only when a field is accessed.
+* ``"reference"``: the reference-compatible launchers of include/dexmpm.h
+  (AoS arrays, dense grid), launch for launch the reference's schedule.
+
+Both keep the reference's memory model (one state per substep, gradients
+accumulated into ``states[i].*_grad``).  Differences: no yacs config (keyword
+arguments, ``cfg`` accepted and ignored except for ``gravity`` /
+``ground_friction`` attributes), and device-side pose copies (``set_pose``
+accepts device tensors without a host round trip).
 
 For throughput (many environments, checkpointed gradients, CUDA graphs) use
-dexdeform_gb300.engine / dexdeform_gb300.torch_wrapper instead.
+dexdeform_gb300.engine / dexdeform_gb300.torch_wrapper.
 """
 from __future__ import annotations
 
@@ -90,20 +101,76 @@ class DeviceArray:
         self.t[:v.shape[0]].add_(v)
 
 
-class TempState:
-    """mpm/simulator.py:46-85: dense scratch grid and per-particle SVD temps."""
+class PlaneArray:
+    """One per-particle field of one state held in SoA planes (the batched
+    engine's slot layout), with the interface of mpm/types.py:294-400
+    ``array``: ``.t`` is an (n, 3) or (n, 3, 3) strided view of the planes
+    (reads and writes go to the planes); upload / download / zero /
+    cuda_add act through it.  There is no AoS device pointer."""
 
-    def __init__(self, n_particles, grid_dim, n_bodies):
+    def __init__(self, planes: torch.Tensor, shape):
+        self.planes = planes      # (width, stride) view of a state slot
+        self._shape = tuple(shape)
+
+    @property
+    def t(self):
+        v = self.planes[:, :self._shape[0]].t()
+        return v.view(self._shape) if len(self._shape) == 3 else v
+
+    @property
+    def shape(self):
+        return self._shape
+
+    @property
+    def data_ptr(self):
+        raise N.DexError("state fields of the batched backend are SoA planes: use .t (or backend='reference')")
+
+    def upload(self, arr, strict=False):
+        a = torch.as_tensor(np.asarray(arr) if not isinstance(arr, torch.Tensor) else arr)
+        a = a.to(device=self.planes.device, dtype=torch.float32).reshape((-1,) + self._shape[1:])
+        n = a.shape[0]
+        if strict:
+            assert n == self._shape[0]
+        assert n <= self._shape[0], f"{n} {self._shape[0]}"
+        self.t[:n].copy_(a)
+
+    upload_async = upload
+
+    def download(self, n=None, device="numpy", stream=None):
+        src = self.t if n is None else self.t[:n]
+        if device == "numpy":
+            return src.detach().cpu().numpy().copy()
+        return src.detach().to(device).contiguous()
+
+    def zero(self, stream=None):
+        self.planes.zero_()
+
+    zero_async = zero
+
+    def cuda_add(self, values, stream=None):
+        v = torch.as_tensor(values, dtype=torch.float32, device=self.planes.device).reshape((-1,) + self._shape[1:])
+        self.t[:v.shape[0]].add_(v)
+
+
+class TempState:
+    """mpm/simulator.py:46-85: dense scratch grid and per-particle SVD temps
+    (full=False: only what the loss hooks use -- the batched backend keeps
+    its grids in the engine)."""
+
+    def __init__(self, n_particles, grid_dim, n_bodies, full=True):
         g = int(grid_dim[0] * grid_dim[1] * grid_dim[2])
         A = DeviceArray
-        self.grid_m, self.grid_v_in, self.grid_v_out = A((g,)), A((g, 3)), A((g, 3))
-        self.grid_m_grad, self.grid_v_in_grad, self.grid_v_out_grad = A((g,)), A((g, 3)), A((g, 3))
+        self.grid_m, self.grid_m_grad = A((g,)), A((g,))
+        self.grid_lower = DeviceArray((1, 3), dtype=torch.int32)
+        if not full:
+            return
+        self.grid_v_in, self.grid_v_out = A((g, 3)), A((g, 3))
+        self.grid_v_in_grad, self.grid_v_out_grad = A((g, 3)), A((g, 3))
         self.grid_body_v_in = A((g * (n_bodies + 1), 3))
         self.F, self.U, self.V, self.sig = A((n_particles, 3, 3)), A((n_particles, 3, 3)), A((n_particles, 3, 3)), \
             A((n_particles, 3))
         self.F_grad, self.U_grad, self.V_grad, self.sig_grad = A((n_particles, 3, 3)), A((n_particles, 3, 3)), \
             A((n_particles, 3, 3)), A((n_particles, 3))
-        self.grid_lower = DeviceArray((1, 3), dtype=torch.int32)
 
     def clear(self, stream=None):
         self.grid_m.zero()
@@ -117,7 +184,8 @@ class TempState:
 
 
 class State:
-    """mpm/simulator.py:88-145: one substep's particle and body state (+grads)."""
+    """mpm/simulator.py:88-145: one substep's particle and body state (+grads),
+    AoS device arrays (the reference backend)."""
 
     def __init__(self, n_particles, n_bodies):
         self.n_particles, self.n_bodies = int(n_particles), n_bodies
@@ -148,14 +216,37 @@ class State:
             a.zero()
 
 
+class SoAState(State):
+    """One substep's state in the batched backend: particle fields and their
+    gradients are PlaneArray views of state slot `index` of the simulator's
+    SoA storage (x 0-2, v 3-5, F 6-14, C 15-23); body poses as in State."""
+
+    def __init__(self, sim, index):
+        self.n_particles, self.n_bodies = sim.max_particles, sim.n_bodies
+        self.index = index
+        self.slot, self.gslot = sim._soa[index], sim._soa_grad[index]
+        n = sim.max_particles
+        P = PlaneArray
+        self.x, self.v = P(self.slot[0:3], (n, 3)), P(self.slot[3:6], (n, 3))
+        self.F, self.C = P(self.slot[6:15], (n, 3, 3)), P(self.slot[15:24], (n, 3, 3))
+        self.x_grad, self.v_grad = P(self.gslot[0:3], (n, 3)), P(self.gslot[3:6], (n, 3))
+        self.F_grad, self.C_grad = P(self.gslot[6:15], (n, 3, 3)), P(self.gslot[15:24], (n, 3, 3))
+        nb = max(sim.n_bodies, 1)
+        A = DeviceArray
+        self.body_pos, self.body_rot = A((nb, 3)), A((nb, 4))
+        self.body_pos_grad, self.body_rot_grad = A((nb, 3)), A((nb, 4))
+
+
 class MPMSimulator:
     """mpm/simulator.py:151-634."""
 
     def __init__(self, n_bodies, cfg=None, ground_friction=0., gravity=(0., -1., 0.), n_particles=20000,
                  dx=1. / 64, dt=0.0001, grid_size=(1., 1., 1.), max_steps=30, substeps=20, yield_stress=30.,
-                 vol=(1. / 64 / 2) ** 2, mass=(1. / 64 / 2) ** 2, E=5000., nu=0.2):
+                 vol=(1. / 64 / 2) ** 2, mass=(1. / 64 / 2) ** 2, E=5000., nu=0.2, backend="batched"):
         N.require_cuda()
         self.lib = N.load()
+        assert backend in ("batched", "reference")
+        self.backend = backend
         self._cfg = SimpleNamespace(gravity=tuple(getattr(cfg, "gravity", gravity)),
                                     ground_friction=float(getattr(cfg, "ground_friction", ground_friction)))
         self.dx, self.inv_dx, self.dt = float(dx), 1.0 / float(dx), float(dt)
@@ -176,9 +267,20 @@ class MPMSimulator:
         self.dists_grad = DeviceArray((self.n_particles * max(n_bodies, 1),))
         self.body_type_mu_softness_round = DeviceArray((max(n_bodies, 1), 4))
         self.body_args = DeviceArray((max(n_bodies, 1), 4))
-        self.temp = TempState(self.n_particles, grid_dim, self.n_bodies)
+        batched = backend == "batched"
+        self.temp = TempState(self.n_particles, grid_dim, self.n_bodies, full=not batched)
         self.max_steps = max_steps
-        self.states = [State(self.n_particles, n_bodies) for _ in range(max_steps)]
+        if batched:
+            stride = max(32, (self.n_particles + 31) // 32 * 32)
+            self._soa = torch.zeros((max_steps, N.STATE_PLANES, stride), device="cuda")
+            self._soa_grad = torch.zeros_like(self._soa)
+            self.states = [SoAState(self, i) for i in range(max_steps)]
+            nb = max(n_bodies, 1)
+            self._pose = torch.zeros((substeps + 1, nb, 8), device="cuda")
+            self._bgrad = torch.zeros((2, nb, 8), device="cuda")
+            self._E = None  # batched engine, built on first use (material and bodies are set after __init__)
+        else:
+            self.states = [State(self.n_particles, n_bodies) for _ in range(max_steps)]
         self.stream0 = torch.cuda.current_stream()
         self.stream1 = torch.cuda.current_stream()
         mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
@@ -196,6 +298,40 @@ class MPMSimulator:
     def _run(self, rc, what):
         N.check(rc, what)
 
+    # ------------------------------------------------------ batched engine
+    def _invalidate(self):
+        """Material, bodies or the particle count changed: the batched engine
+        is rebuilt on its next use."""
+        if getattr(self, "backend", "reference") == "batched":
+            self._E = None
+
+    def _engine(self):
+        """One-env BatchEngine over the SoA storage (plane stride of
+        max_particles), from the simulator's current material and bodies."""
+        if self._E is None:
+            from .engine import BatchEngine, EnvSpec
+            n, nb = self.n_particles, self.n_bodies
+            mly = self.particle_mu_lam_yield.download(n)
+            spec = EnvSpec(n=n, grid_dim=tuple(int(g) for g in self.grid_dim), dx=self.dx, dt=self.dt,
+                           gravity=tuple(float(g) * 30 for g in self._cfg.gravity),
+                           ground_friction=self.get_ground_friction(),
+                           body_tfsr=self.body_type_mu_softness_round.download()[:nb],
+                           body_args=self.body_args.download()[:nb], mass=self.particle_mass.download(n),
+                           vol=self.particle_vol.download(n), mu_lam_yield=mly,
+                           ground_height=self.get_ground_height())
+            self._E = BatchEngine([spec], grad=True, stride=self._soa.shape[-1])
+            assert self._E.n_particles == self._soa.shape[-1]
+            self._gtmp = self._E.new_slots(1)[0]
+        return self._E
+
+    def _pack_pose(self, state, out):
+        """Body pose of a state in the engine's [n_bodies][8] layout."""
+        nb = self.n_bodies
+        if nb:
+            out[:nb, :3].copy_(state.body_pos.t[:nb])
+            out[:nb, 4:].copy_(state.body_rot.t[:nb])
+        return out
+
     # ------------------------------------------------------- state access
     def clear_grad(self, max_steps):
         for i in range(max_steps):
@@ -207,6 +343,8 @@ class MPMSimulator:
 
     def set_state(self, index, state):
         state = [np.float32(i) for i in state]
+        if int(len(state[0])) != self.n_particles:
+            self._invalidate()
         self.n_particles = int(len(state[0]))
         pos = np.float32([i[:3] for i in state[4:]]).reshape(-1, 3)
         rot = np.float32([i[3:] for i in state[4:]]).reshape(-1, 4)
@@ -232,6 +370,7 @@ class MPMSimulator:
         pp = self.body_type_mu_softness_round.download()
         pp[:, 2] = softness
         self.body_type_mu_softness_round.upload(pp)
+        self._invalidate()
 
     def get_softness(self):
         return self.body_type_mu_softness_round.download()[:, 2]
@@ -264,6 +403,7 @@ class MPMSimulator:
         self.particle_mu_lam_yield.upload(mu_lam_yield)
         self.gravity.upload(np.float32([np.array(self._cfg.gravity) * 30]))  # mpm/simulator.py:385
         self.temp.grid_lower.upload(GRID_LOWER_ZERO)
+        self._invalidate()
 
     def init_bodies(self, types, softness, mu, round, args, action_scales, pos=None, rot=None):
         assert len(mu) == len(args) == self.n_bodies
@@ -271,6 +411,7 @@ class MPMSimulator:
             np.stack((np.float32(types), np.float32(mu), np.float32(softness), np.float32(round)), 1).reshape(-1, 4))
         self.body_args.upload(np.float32(args))
         self.action_scales = action_scales
+        self._invalidate()
         if pos is not None:
             self.states[0].body_pos.upload(np.array(pos).reshape(self.n_bodies, 3))
         if rot is not None:
@@ -355,6 +496,13 @@ class MPMSimulator:
 
     def substep(self, f, clear_grad=False):
         """mpm/simulator.py:561-571"""
+        if self.backend == "batched":
+            cur, nxt = self.states[f], self.states[f + 1]
+            E = self._engine()
+            E.substep(cur.slot, nxt.slot, self._pack_pose(cur, self._pose[0]), self._pack_pose(nxt, self._pose[1]))
+            if clear_grad:
+                nxt.clear_grad()
+            return
         temp, cur, nxt = self.temp, self.states[f], self.states[f + 1]
         temp.clear()
         self.compute_svd(cur, temp)
@@ -365,7 +513,23 @@ class MPMSimulator:
             nxt.clear_grad()
 
     def substep_grad(self, f):
-        """mpm/simulator.py:573-585"""
+        """mpm/simulator.py:573-585: the gradients of state f + 1 back to
+        state f and to both body poses, added to what they hold."""
+        if self.backend == "batched":
+            cur, nxt = self.states[f], self.states[f + 1]
+            E = self._engine()
+            bg = self._bgrad
+            bg.zero_()
+            E.substep_grad(cur.slot, nxt.slot, nxt.gslot, self._gtmp, self._pack_pose(cur, self._pose[0]),
+                           self._pack_pose(nxt, self._pose[1]), bg[0], bg[1])
+            cur.gslot.add_(self._gtmp)
+            nb = self.n_bodies
+            if nb:
+                cur.body_pos_grad.t[:nb].add_(bg[0, :nb, :3])
+                cur.body_rot_grad.t[:nb].add_(bg[0, :nb, 4:])
+                nxt.body_pos_grad.t[:nb].add_(bg[1, :nb, :3])
+                nxt.body_rot_grad.t[:nb].add_(bg[1, :nb, 4:])
+            return
         temp, cur, nxt = self.temp, self.states[f], self.states[f + 1]
         temp.clear()
         temp.clear_grad()
@@ -378,6 +542,21 @@ class MPMSimulator:
         self.compute_svd_grad(cur, temp)
 
     # ------------------------------------------------------- loss hooks
+    def _aos(self, state, n=None):
+        """(x, x_grad) device pointers of the first n particles of a state for
+        the AoS loss-hook launchers, and a finisher that adds an AoS x
+        gradient back (batched backend: contiguous copies of the planes)."""
+        if self.backend != "batched":
+            return state.x.data_ptr, state.x_grad.data_ptr, lambda: None
+        n = self.n_particles if n is None else int(n)
+        x = state.x.t[:n].contiguous()
+        gx = torch.zeros_like(x)
+        self._aos_keep = (x, gx)
+
+        def finish():
+            state.x_grad.t[:n].add_(gx)
+        return ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(gx.data_ptr()), finish
+
     def get_dists(self, f, grad=None, device="cuda:0"):
         """mpm/simulator.py:294-321 (compute_dist, integrator.cu:188-237)."""
         state = self.states[f]
@@ -385,12 +564,15 @@ class MPMSimulator:
         if need_grad:
             assert grad.shape == (self.n_particles, self.n_bodies)
             self.dists_grad.t[:grad.numel()].copy_(torch.as_tensor(grad).reshape(-1))
-        self._run(self.lib.compute_dist(state.x.data_ptr, state.body_pos.data_ptr, state.body_rot.data_ptr,
+        x_ptr, gx_ptr, finish = self._aos(state)
+        self._run(self.lib.compute_dist(x_ptr, state.body_pos.data_ptr, state.body_rot.data_ptr,
                                         self.body_type_mu_softness_round.data_ptr, self.body_args.data_ptr,
-                                        self.dists.data_ptr, self.n_bodies, state.x_grad.data_ptr,
+                                        self.dists.data_ptr, self.n_bodies, gx_ptr,
                                         state.body_pos_grad.data_ptr, state.body_rot_grad.data_ptr,
                                         self.dists_grad.data_ptr, int(need_grad), self.n_particles, self._sp()),
                   "compute_dist")
+        if need_grad:
+            finish()
         if not need_grad:
             return self.dists.download(self.n_particles * self.n_bodies, device=device).reshape(-1, self.n_bodies)
 
@@ -410,11 +592,14 @@ class MPMSimulator:
         if need_grad:
             self.temp.grid_m_grad.t.copy_(torch.as_tensor(backward_grad).reshape(-1))
         self.temp.grid_m.zero()
-        self._run(self.lib.particle2mass(state.x.data_ptr, self.particle_mass.data_ptr, self.temp.grid_lower.data_ptr,
+        x_ptr, gx_ptr, finish = self._aos(state, n_particles)
+        self._run(self.lib.particle2mass(x_ptr, self.particle_mass.data_ptr, self.temp.grid_lower.data_ptr,
                                          ctypes.cast(self.grid_dim, ctypes.c_void_p), self.dx, self.inv_dx,
                                          self.temp.grid_m.data_ptr, self.temp.grid_m_grad.data_ptr,
-                                         state.x_grad.data_ptr, self.particle_ids.data_ptr, id, int(need_grad),
+                                         gx_ptr, self.particle_ids.data_ptr, id, int(need_grad),
                                          n_particles, self._sp()), "particle2mass")
+        if need_grad:
+            finish()
         if not need_grad:
             return self.temp.grid_m.download(device=device).reshape(*list(self.grid_dim))
 
@@ -439,10 +624,18 @@ class MPMSimulator:
         return pos, rot, (pos, rot)
 
     def step(self, action, pos_rot=None):
-        """mpm/simulator.py:626-634"""
+        """mpm/simulator.py:626-634 (batched backend: the env step's substeps
+        in one fused sequence, each G2P fused with the next P2G)."""
         pos, rot, _ = self.compute_forward_kinematics(self.cur, action, pos_rot=pos_rot)
         for f in range(self.substeps):
             self.set_pose(self.states[f + 1], pos[f], rot[f])
-            self.substep(f)
+        if self.backend == "batched":
+            T = self.substeps
+            for f in range(T + 1):
+                self._pack_pose(self.states[f], self._pose[f])
+            self._engine().run_substeps([self.states[f].slot for f in range(T + 1)], self._pose[:T + 1])
+        else:
+            for f in range(self.substeps):
+                self.substep(f)
         self.sync()
         self.states[0], self.states[self.substeps] = self.states[self.substeps], self.states[0]

@@ -34,10 +34,13 @@ class DiffSim:
     """Differentiable batched simulator core: T substeps per env step.  The
     adjoint recomputes the env step from its input state into a ring of T+1
     state slots, keeping each substep's grid slot, then runs the adjoint
-    kernels in reverse on those slots."""
+    kernels in reverse on those slots.  With `sort` (default) each call first
+    orders the particles by grid cell on the device (BatchEngine.sort) and
+    maps the results back: states and gradients go in and out in the
+    caller's order."""
 
     def __init__(self, specs: Sequence[EnvSpec], substeps: int, device="cuda", tile_size=128, use_graphs=True,
-                 capsule_grad="reference"):
+                 capsule_grad="reference", sort=True):
         self.T = int(substeps)
         self.E = BatchEngine(specs, device=device, grad=True, tile_size=tile_size, capsule_grad=capsule_grad,
                              grid_slots=self.T + 2)
@@ -49,33 +52,62 @@ class DiffSim:
         self.poses = torch.zeros((self.T + 1, self.nb, 8), device=dev)
         self.bgrad = torch.zeros((self.T + 1, self.nb, 8), device=dev)
         self.use_graphs = use_graphs
+        self.sort = bool(sort)
+        self.src = self.E.new_slots(1)[0]   # input state, caller's order
+        self.io = self.E.new_slots(1)[0]    # output state / gradient, caller's order
+        if self.sort:
+            self.perm = self.E.identity_perm(1)[0]
+            self.mat = self.E.mat.clone()
         self._g = {}
+
+    def _prepare(self):
+        """ring[0] = the input state in the order the substeps run in."""
+        E = self.E
+        if self.sort:
+            E.sort(self.src, self.ring[0], self.perm)
+            E.permute(self.perm, E.mat, self.mat)
+            E.use_material(self.mat)
+        else:
+            self.ring[0].copy_(self.src)
+            E.use_material()
 
     # eager bodies of the two graphs
     def _fwd(self):
+        self._prepare()
         self.E.run_substeps([self.ring[s] for s in range(self.T + 1)], self.poses)
+        if self.sort:
+            self.E.permute(self.perm, self.ring[self.T], self.io, inverse=True)
+        else:
+            self.io.copy_(self.ring[self.T])
 
     def _bwd(self):
         E = self.E
+        self._prepare()
+        if self.sort:
+            E.permute(self.perm, self.io, self.gbuf[1])
+        else:
+            self.gbuf[1].copy_(self.io)
         E.run_substeps([self.ring[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
         out = E.run_adjoint([self.ring[s] for s in range(self.T + 1)], self.gbuf[1], self.gbuf[0], self.poses,
                             self.bgrad, tapes=self.tape)
-        if out is not self.gbuf[1]:
-            self.gbuf[1].copy_(out)
+        if self.sort:
+            E.permute(self.perm, out, self.io, inverse=True)
+        else:
+            self.io.copy_(out)
 
     def forward(self, state: torch.Tensor, poses: torch.Tensor) -> torch.Tensor:
-        self.ring[0].copy_(state)
+        self.src.copy_(state)
         self.poses.copy_(poses)
         run_graph(self.E, self._g, "fwd", self._fwd, self.use_graphs)
-        return self.ring[self.T].clone()
+        return self.io.clone()
 
     def backward(self, state: torch.Tensor, poses: torch.Tensor, g_out: torch.Tensor):
-        self.ring[0].copy_(state)
+        self.src.copy_(state)
         self.poses.copy_(poses)
-        self.gbuf[1].copy_(g_out)
+        self.io.copy_(g_out)
         self.bgrad.zero_()
         run_graph(self.E, self._g, "bwd", self._bwd, self.use_graphs)
-        return self.gbuf[1].clone(), self.bgrad.clone()
+        return self.io.clone(), self.bgrad.clone()
 
 
 class EnvStep(torch.autograd.Function):
@@ -182,12 +214,12 @@ class GradModel:
     does with the observation gradients)."""
 
     def __init__(self, env, hand, substeps, return_grid=(), device="cuda", use_graphs=True,
-                 capsule_grad="reference"):
+                 capsule_grad="reference", sort=True):
         self.env = env
         self.hand = hand
         self.device = torch.device(device)
         self.sim = DiffSim([EnvSpec.from_env(env)], substeps, device=device, use_graphs=use_graphs,
-                           capsule_grad=capsule_grad)
+                           capsule_grad=capsule_grad, sort=sort)
         E = self.sim.E
         self.n, self.nb = env.n, env.nb
         self.tfsr = torch.tensor(env.body_tfsr, device=self.device)

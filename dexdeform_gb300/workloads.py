@@ -201,8 +201,9 @@ def batch_envs(seed=0, n_envs=64, steps=50, n_lo=2000, n_hi=30000, grid=64, sort
     return envs
 
 
-def large_env(seed=0, steps=100, n=300000):
-    """Large: 128^3, dt 2.5e-5, two stacked cubes (yield 40 / 120), 22 capsules + palm box."""
+def large_env(seed=0, steps=100, n=300000, sort=True):
+    """Large: 128^3, dt 2.5e-5, two stacked cubes (yield 40 / 120), 22 capsules + palm box.
+    sort=False keeps the sampling order (the two cubes one after the other)."""
     rng = np.random.default_rng(seed)
     grid, dt = 128, 2.5e-5
     dx = 1.0 / grid
@@ -211,8 +212,9 @@ def large_env(seed=0, steps=100, n=300000):
     x2, v2 = sample_cube(rng, n - n1, (0.5, 0.35, 0.5), 0.2)
     x = np.concatenate([x1, x2])
     ys = np.concatenate([np.full(n1, 40.0), np.full(n - n1, 120.0)]).astype(np.float32)
-    order = cell_sort(x, dx)
-    x, ys = x[order], ys[order]
+    if sort:
+        order = cell_sort(x, dx)
+        x, ys = x[order], ys[order]
     mu, lam = lame()
     pv = (v1 + v2) / n
     tfsr, args = capsules(rng, 23)

@@ -306,6 +306,48 @@ int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *next_s, con
                            const float *mu_lam_yield, const float *body_shape, const float *pose,
                            const float *next_pose, int32_t *error, dexmpm_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Particle order.  The scatters pre-reduce a warp's contributions per stencil
+ * base, which pays when particles that are close in space are close in
+ * memory.  dexmpm_sort re-orders every env's particles (within the env's
+ * range) by the 4^3 block of their stencil base cell, then by the cell
+ * within the block, then by their previous index: a counting sort in one
+ * launch per phase for all envs.  No counterpart in the reference, which
+ * scatters in the caller's order (mpm/csrc/integrator.cu:312-394).
+ *
+ * DexSortWork: caller-owned device scratch, all zero before the first sort
+ * (each sort leaves cell_count, block_total, block_flag and counters zero). */
+#define DEXMPM_STATE_PLANES 24
+#define DEXMPM_SORT_CHUNK 4096 /* block totals per scan CTA */
+#define DEXMPM_SORT_PARTIALS(n_blocks) (((n_blocks) + DEXMPM_SORT_CHUNK - 1) / DEXMPM_SORT_CHUNK)
+typedef struct {
+  int32_t *cell_count;  /* [n_blocks * 64] */
+  int32_t *cell_start;  /* [n_blocks * 64] */
+  int32_t *block_total; /* [n_blocks] */
+  int32_t *block_base;  /* [n_blocks] */
+  uint32_t *block_flag; /* [n_blocks] */
+  int32_t *block_list;  /* [n_blocks] */
+  int32_t *rank;        /* [n_particles] */
+  int32_t *key;         /* [n_particles] */
+  int32_t *partial;     /* [DEXMPM_SORT_PARTIALS(n_blocks)] */
+  int32_t *counters;    /* [4] */
+} DexSortWork;
+
+/* Sort the particles of state slot s: perm[i] = the index in s of the
+ * particle that goes to index i (entries of the padding beyond the envs'
+ * particles are left as they are: initialise perm to the identity once), and
+ * sorted_s = s gathered by perm (24 planes).  s and sorted_s must differ.  At
+ * most 4,194,304 grid blocks. */
+int dexmpm_sort(const DexBatch *b, const DexSortWork *w, const float *s, float *sorted_s, int32_t *perm,
+                dexmpm_stream_t stream);
+
+/* Apply a permutation to `planes` planes of n 32-bit words (floats or
+ * int32): inverse = 0 gathers dst[q][i] = src[q][perm[i]] (into the sorted
+ * order), inverse = 1 scatters dst[q][perm[i]] = src[q][i] (back to the
+ * previous order, e.g. gradients).  src and dst must differ. */
+int dexmpm_permute(const int32_t *perm, const void *src, void *dst, int n, int planes, int inverse,
+                   dexmpm_stream_t stream);
+
 /* Copy out and clear the device error word (host pointer out). */
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream);
 

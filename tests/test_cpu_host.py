@@ -33,14 +33,15 @@ def test_struct_layouts_match_header():
     src = os.path.join(tempfile.mkdtemp(), "l.c")
     with open(src, "w") as f:
         f.write('#include <stdio.h>\n#include <stddef.h>\n#include "dexmpm.h"\nint main(){'
-                'printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(DexEnv), offsetof(DexEnv, gravity), '
+                'printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(DexEnv), offsetof(DexEnv, gravity), '
                 'sizeof(DexBatch), offsetof(DexBatch, grid), offsetof(DexBatch, block_count), '
-                'offsetof(DexBatch, error)); return 0;}\n')
+                'offsetof(DexBatch, error), sizeof(DexSortWork), offsetof(DexSortWork, partial)); return 0;}\n')
     exe = src[:-2]
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
     got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(N.DexEnv), N.DexEnv.gravity.offset, ctypes.sizeof(N.DexBatch), N.DexBatch.grid.offset,
-            N.DexBatch.block_count.offset, N.DexBatch.error.offset]
+            N.DexBatch.block_count.offset, N.DexBatch.error.offset, ctypes.sizeof(N.DexSortWork),
+            N.DexSortWork.partial.offset]
     assert got == want
 
 
@@ -346,3 +347,27 @@ def test_render_launchers_reject_bad_arguments(native_lib):
     assert native_lib.render(*args, 0.4, g, 65, True, im, 2, 1, 0.0, 0, one, P) != 0   # > 64 bodies
     assert native_lib.render(*args, 0.4, g, 1, True, im, 2, 0, 0.0, 0, one, P) != 0    # spp 0
     assert native_lib.render(*args[:11], P, one, 0.4, g, 1, True, im, 2, 1, 0.0, 0, one, P) != 0  # no color buffer
+
+
+def test_sort_entry_points_check_arguments(native_lib):
+    """dexmpm_sort / dexmpm_permute reject bad arguments before any CUDA call
+    and return OK without a launch when there is nothing to move."""
+    import ctypes
+    from dexdeform_gb300 import _native as N
+    one, two = ctypes.c_void_p(1), ctypes.c_void_p(2)
+    b = N.DexBatch()
+    b.n_envs, b.n_particles, b.n_tiles, b.n_blocks, b.tile_size = 1, 32, 1, 8, 128
+    b.envs, b.tiles = 1, 1
+    w = N.DexSortWork()
+    for f, _ in N.DexSortWork._fields_:
+        setattr(w, f, 1)
+    sort, perm = native_lib.dexmpm_sort, native_lib.dexmpm_permute
+    assert sort(None, ctypes.byref(w), one, two, one, None) == N.ERR_ARG          # no batch
+    assert sort(ctypes.byref(b), None, one, two, one, None) == N.ERR_ARG          # no scratch
+    assert sort(ctypes.byref(b), ctypes.byref(w), one, one, one, None) == N.ERR_ARG  # in place
+    w.rank = None
+    assert sort(ctypes.byref(b), ctypes.byref(w), one, two, one, None) == N.ERR_ARG  # incomplete scratch
+    assert perm(one, one, one, 32, 24, 0, None) == N.ERR_ARG                        # in place
+    assert perm(None, one, two, 32, 24, 0, None) == N.ERR_ARG                       # no permutation
+    assert perm(one, one, two, -1, 24, 0, None) == N.ERR_ARG                        # negative size
+    assert perm(one, one, two, 0, 24, 0, None) == N.OK                              # nothing to move

@@ -124,10 +124,11 @@ def test_batched_adjoint_vs_oracle(cuda, oracle_mod, name):
     assert E.error_word() == 0
 
 
-def _abi_sim(env, steps):
+def _abi_sim(env, steps, backend="reference"):
     from dexdeform_gb300.simulator import MPMSimulator
     sim = MPMSimulator(env.nb, n_particles=env.n, dx=env.dx, dt=env.dt, grid_size=tuple(g * env.dx for g in env.grid_dim),
-                       max_steps=steps + 1, substeps=steps, gravity=(0, -1, 0), ground_friction=env.ground_friction)
+                       max_steps=steps + 1, substeps=steps, gravity=(0, -1, 0), ground_friction=env.ground_friction,
+                       backend=backend)
     sim.init_particles(env.vol.astype(np.float64), env.mass.astype(np.float64), env.mu_lam_yield.astype(np.float64))
     sim.init_bodies(env.body_tfsr[:, 0], env.body_tfsr[:, 2], env.body_tfsr[:, 1], env.body_tfsr[:, 3],
                     env.body_args, None)
@@ -138,16 +139,24 @@ def _abi_sim(env, steps):
     return sim
 
 
-def test_reference_abi_forward(cuda, oracle_mod):
-    """The drop-in launchers in the reference's schedule (MPMSimulator.substep)."""
+@pytest.mark.parametrize("backend", ["reference", "batched"])
+def test_reference_abi_forward(cuda, oracle_mod, backend):
+    """The drop-in MPMSimulator in the reference's schedule (substep by
+    substep): on the reference-compatible launchers, against the oracle with
+    the reference's SVD; on the batched kernels, against the exact one with
+    the bars of the batched forward tests."""
     env, z = golden_env(os.path.join(GOLDEN, "ref_forward_32.npz"))
-    sim = _abi_sim(env, 20)
+    sim = _abi_sim(env, 20, backend)
     for f in range(20):
         sim.substep(f)
-    rf = oracle_rollout(oracle_mod, env, 20, "reference")
+    rf = oracle_rollout(oracle_mod, env, 20, "reference" if backend == "reference" else "exact")
     for t in (1, 20):
         x, v, F, C = sim.get_state(t)[:4]
         got = {"x": x, "v": v, "F": F, "C": C}
+        if backend == "batched":
+            for k in ("x", "v", "F", "C"):
+                assert rel(got[k], rf[t][k]) < (1e-5 if t == 1 and k in "xF" else 5e-4 if t == 1 else 1e-3), (t, k)
+            continue
         for k in ("x", "F"):
             assert rel(got[k], rf[t][k]) < 1e-5, (t, k)
         for k in ("v", "C"):
@@ -155,10 +164,42 @@ def test_reference_abi_forward(cuda, oracle_mod):
             assert rel(got[k], z[f"s{t}_{k}"]) < 5e-3, (t, k)
 
 
-def test_reference_abi_adjoint(cuda, oracle_mod):
+def test_simulator_batched_backend_equals_engine(cuda):
+    """The drop-in MPMSimulator on the batched backend: substep by substep
+    and the fused env step (step) give the BatchEngine's results, and
+    get_state/set_state keep the reference's tuple layout."""
+    from dexdeform_gb300 import workloads as W
+    env = W.make_env(9, 3000, "cube", grid=64, center=(0.5, 0.15, 0.5), extent=0.2, steps=10, sort=False)
+    want = batched_rollout(env, 10)
+    for mode in ("substep", "step"):
+        sim = _abi_sim(env, 10, "batched")
+        if mode == "substep":
+            for f in range(10):
+                sim.substep(f)
+        else:
+            # step() integrates per-substep poses from a 6-D action per body;
+            # drive it with the env's poses instead through set_pose
+            for f in range(10):
+                sim.set_pose(sim.states[f + 1], env.poses[f + 1][:, :3], env.poses[f + 1][:, 3:])
+            T = 10
+            for f in range(T + 1):
+                sim._pack_pose(sim.states[f], sim._pose[f])
+            sim._engine().run_substeps([sim.states[f].slot for f in range(T + 1)], sim._pose[:T + 1])
+        st = sim.get_state(10)
+        assert len(st) == 4 + env.nb and st[4].shape == (7,)
+        # the same kernels and launches (substep), or G2P fused with the next
+        # P2G (step): float-atomic ordering only
+        for k, i in (("x", 0), ("v", 1), ("F", 2), ("C", 3)):
+            assert rel(st[i], want[10][k]) < (1e-5 if mode == "substep" else 1e-4), (mode, k)
+        assert sim.get_x(10).shape == (env.n, 3)
+        assert sim._engine().error_word() == 0
+
+
+@pytest.mark.parametrize("backend", ["reference", "batched"])
+def test_reference_abi_adjoint(cuda, oracle_mod, backend):
     env, z = golden_env(os.path.join(GOLDEN, "ref_grad_32.npz"))
     env.x, env.v, env.F, env.C = z["in_x"], z["in_v"], z["in_F"], z["in_C"]
-    sim = _abi_sim(env, 1)
+    sim = _abi_sim(env, 1, backend)
     sim.substep(0)
     s1 = sim.states[1]
     s1.x_grad.upload(z["gnext_x"])
@@ -176,16 +217,20 @@ def test_reference_abi_adjoint(cuda, oracle_mod):
     og, (bp, br), (nbp, nbr) = o.substep_grad(st, env.pose(0), env.pose(1), nx["v"],
                                               {k: z[f"gnext_{k}"] for k in ("x", "v", "F", "C")})
     for k in ("x", "v", "F", "C"):
-        assert rel(got[k], og[k]) < 2e-4, k
+        assert rel(got[k], og[k]) < (2e-4 if backend == "reference" else 1e-4), k
     assert rel(s0.body_pos_grad.download(), bp) < 2e-3
     assert rel(s1.body_pos_grad.download(), nbp) < 2e-3
+    # gradients accumulate, as the reference's kernels do
+    sim.substep_grad(0)
+    assert rel(s0.x_grad.download(), 2 * got["x"]) < 1e-5
 
 
-def test_loss_hooks(cuda, oracle_mod):
+@pytest.mark.parametrize("backend", ["reference", "batched"])
+def test_loss_hooks(cuda, oracle_mod, backend):
     """compute_dist and particle2mass (integrator.cu:188-310) and their adjoints."""
     from dexdeform_gb300 import workloads as W
     env = W.tiny_env(2, n=300, grid=32, nb=5, steps=1, dt=1e-4)
-    sim = _abi_sim(env, 1)
+    sim = _abi_sim(env, 1, backend)
     o = oracle_sim(oracle_mod, env)
     d = sim.get_dists(0, device="numpy")
     assert rel(d, o.compute_dist(env.x, env.pose(0))) < 1e-5
