@@ -379,9 +379,15 @@ def kernel_times(E, R, s0, g_final):
     # the material), and the gradient's way back through it, as a rollout
     # runs them once per env step
     if R._sorted:
+        # the first boundary sorts the caller's sampling order (a random
+        # permutation); later ones re-sort the end of an env step (50
+        # substeps of drift: nearly in order)
         perm = E.identity_perm(1)[0]
         mat = torch.empty_like(E.mat)
-        timed("sort", lambda: E.sort(R.src, ring[1], perm))
+        timed("sort_initial", lambda: E.sort(R.src, ring[1], perm))
+        timed("permute_grad_initial", lambda: E.permute(perm, ring[1], ring[2], inverse=True))
+        drifted = R.stored(R.S) if R.S > 1 else ck[0]
+        timed("sort", lambda: E.sort(drifted, ring[1], perm))
         timed("permute_material", lambda: E.permute(perm, E.mat, mat))
         timed("permute_grad", lambda: E.permute(perm, ring[1], ring[2], inverse=True))
     E.use_material(R.material(0))
@@ -445,6 +451,8 @@ def kernel_times(E, R, s0, g_final):
 # Algorithmic bytes per particle (N) and per cell of the active blocks (A)
 # for each kernel: particle state read/written once, grid float4 cells once.
 ALG_BYTES = {
+    "sort_initial": (236, 0),  # as "sort", from a random order
+    "permute_grad_initial": (196, 0),
     "sort": (236, 0),          # x read, key + rank written and read, perm written and segment-sorted; 24 planes
                                # gathered (96 B read, 96 B written, perm read)
     "permute_material": (44, 0),  # 5 material planes gathered, perm read
@@ -477,7 +485,8 @@ NCU_L2_RED = {"g2p2g": (3212980, 5181759, 10.93), "g2p2g_tape": (3215606, 518504
 
 # kernel function of each timed launch variant (the forward pass and the
 # recompute launch the same function, the recompute with the tape written)
-FUNCTION = {"sort": "dexmpm_sort", "permute_material": "k_permute", "permute_grad": "k_permute", "p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape": "k_g2p2g",
+FUNCTION = {"sort_initial": "dexmpm_sort", "permute_grad_initial": "k_permute", "sort": "dexmpm_sort",
+            "permute_material": "k_permute", "permute_grad": "k_permute", "p2g": "k_p2g", "p2g_tape": "k_p2g", "g2p2g": "k_g2p2g", "g2p2g_tape": "k_g2p2g",
             "grid_op": "k_grid_op", "grid_op_keep": "k_grid_op", "g2p": "k_g2p", "g2p_grad": "k_g2p_grad",
             "grid_op_grad": "k_grid_op_grad", "p2g_grad": "k_p2g_grad", "p2g2g_grad": "k_p2g2g_grad"}
 
@@ -485,9 +494,13 @@ FUNCTION = {"sort": "dexmpm_sort", "permute_material": "k_permute", "permute_gra
 # launches per fwd+bwd substep (forward pass + recompute + adjoint; the first
 # P2G and last G2P of an env step of SUBSTEPS substeps stand alone)
 def launches_per_substep(T):
-    return {"sort": 1 / T, "permute_material": 1 / T, "permute_grad": 1 / T, "p2g": 1 / T, "p2g_tape": 1 / T, "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1,
-            "grid_op_keep": 1, "g2p": 2 / T, "g2p_grad": 1 / T, "grid_op_grad": 1, "p2g_grad": 1 / T,
-            "p2g2g_grad": 1 - 1 / T}
+    # (the initial sort and its gradient map run once per rollout of
+    # ENV_STEPS env steps, the others once per later env step)
+    S = ENV_STEPS
+    return {"sort_initial": 1 / (T * S), "permute_grad_initial": 1 / (T * S), "sort": (S - 1) / (T * S),
+            "permute_material": 1 / T, "permute_grad": (S - 1) / (T * S), "p2g": 1 / T, "p2g_tape": 1 / T,
+            "g2p2g": 1 - 1 / T, "g2p2g_tape": 1 - 1 / T, "grid_op": 1, "grid_op_keep": 1, "g2p": 2 / T,
+            "g2p_grad": 1 / T, "grid_op_grad": 1, "p2g_grad": 1 / T, "p2g2g_grad": 1 - 1 / T}
 
 
 def roofline(E, kt, cells):
@@ -672,7 +685,7 @@ def plain_rates(envs, dev, sample_every=8, backend="reference"):
     import torch
     from dexdeform_gb300.simulator import MPMSimulator
     T = SUBSTEPS
-    fwd_t = bwd_t = 0.0
+    fwd_t = bwd_t = step_t = 0.0
     work = 0
     for env in envs[::sample_every]:
         sim = MPMSimulator(env.nb, n_particles=env.n, dx=env.dx, dt=env.dt, grid_size=(1, 1, 1), max_steps=T + 1,
@@ -700,10 +713,25 @@ def plain_rates(envs, dev, sample_every=8, backend="reference"):
         fwd_t += a.elapsed_time(b) / 1e3
         bwd_t += a.elapsed_time(c) / 1e3
         work += env.n * T
+        if backend == "batched":
+            # MPMSimulator.step: the env step's substeps as one fused sequence
+            sim.action_scales = np.full((env.nb, 6), 0.01, np.float32)
+            act = np.zeros((env.nb, 6), np.float32)
+            sim.step(act)
+            torch.cuda.synchronize()
+            a.record()
+            for _ in range(2):
+                sim.step(act)
+            b.record()
+            torch.cuda.synchronize()
+            step_t += a.elapsed_time(b) / 2e3
         del sim
-    return {"fwd": work / fwd_t, "fwd_bwd": work / bwd_t, "unit": UNIT,
-            "what": f"reference schedule through MPMSimulator (backend {backend!r}), one env at a time, "
-                    f"{len(envs[::sample_every])} sampled envs x 1 env step"}
+    out = {"fwd": work / fwd_t, "fwd_bwd": work / bwd_t, "unit": UNIT,
+           "what": f"reference schedule through MPMSimulator (backend {backend!r}), one env at a time, "
+                   f"{len(envs[::sample_every])} sampled envs x 1 env step"}
+    if step_t > 0:
+        out["step"] = work / step_t
+    return out
 
 
 def median_env(envs):

@@ -184,11 +184,17 @@ __global__ void __launch_bounds__(256) k_sort_place(DexBatch B, DexSortWork W, i
 }
 
 // Per occupied cell (a warp per block, two cells per lane): its segment of
-// perm in increasing old index (insertion sort; a few to a few tens of
-// entries), then the cell count, block total and flag cleared.  The last CTA
-// to finish resets the list count and its own ticket.
+// perm in increasing old index, then the cell count, block total and flag
+// cleared.  A segment of up to kFixSeg entries is sorted in the lane's own
+// row of shared memory (insertion sort; one pass when the input was already
+// in order, as after an env step of drift); a longer one in place in global
+// memory.  The last CTA to finish resets the list count and its own ticket.
+constexpr int kFixSeg = 32;
+constexpr int kFixRow = kFixSeg + 1;  // padded: the lanes' rows start in different banks
 __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__restrict__ perm) {
+  __shared__ int32_t rows[256 * kFixRow];
   const int lane = threadIdx.x & 31;
+  int32_t *row = rows + threadIdx.x * kFixRow;
   const int warps = gridDim.x * (blockDim.x >> 5);
   const int cnt = *reinterpret_cast<volatile int32_t *>(W.counters);
   for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < cnt; item += warps) {
@@ -199,14 +205,38 @@ __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__rest
       const int ci = (blk << 6) + 2 * lane + h;
       const int n = W.cell_count[ci];
       int32_t *seg = perm + base + W.cell_start[ci];
-      for (int a = 1; a < n; ++a) {
-        const int32_t v = seg[a];
-        int b = a - 1;
-        while (b >= 0 && seg[b] > v) {
-          seg[b + 1] = seg[b];
-          --b;
+      if (n > 1 && n <= kFixSeg) {
+        bool sorted = true;
+        int32_t prev = seg[0];
+        row[0] = prev;
+        for (int a = 1; a < n; ++a) {
+          const int32_t v = seg[a];
+          sorted = sorted && v > prev;
+          prev = v;
+          row[a] = v;
         }
-        seg[b + 1] = v;
+        if (!sorted) {
+          for (int a = 1; a < n; ++a) {
+            const int32_t v = row[a];
+            int b = a - 1;
+            while (b >= 0 && row[b] > v) {
+              row[b + 1] = row[b];
+              --b;
+            }
+            row[b + 1] = v;
+          }
+          for (int a = 0; a < n; ++a) seg[a] = row[a];
+        }
+      } else if (n > kFixSeg) {
+        for (int a = 1; a < n; ++a) {
+          const int32_t v = seg[a];
+          int b = a - 1;
+          while (b >= 0 && seg[b] > v) {
+            seg[b + 1] = seg[b];
+            --b;
+          }
+          seg[b + 1] = v;
+        }
       }
       W.cell_count[ci] = 0;
     }

@@ -27,6 +27,8 @@ from typing import Dict, List, Optional, Sequence, Tuple
 import numpy as np
 import torch
 
+from .simulator import MPMSimulator
+
 # ------------------------------------------------------------------ tables
 # Joint order of the hand's 24 joints (mpm/robots/interface.py:13-38): the
 # index of a joint in q.
@@ -424,6 +426,25 @@ class ShadowHand:
         args[m.geom_type == 1, 2] = 0.0
         return np.tile(tfsr, (n_hands, 1)), np.tile(args, (n_hands, 1))
 
+    # the hand interface GradModel drives (joint angles at a fixed base pose)
+    def set_base(self, base):
+        """Fixed base pose (4, 4) of fk / joint_velocity_poses."""
+        self.base = torch.as_tensor(np.asarray(base) if not isinstance(base, torch.Tensor) else base,
+                                    dtype=self.M.dtype, device=self.device)
+        return self
+
+    def fk(self, q: torch.Tensor):
+        """Joint angles (24,) at the fixed base -> geom positions (G, 3) and
+        quaternions (G, 4)."""
+        pos, rot = self.forward_kinematics(self.base[None, None], q[None, None])
+        return pos[0], rot[0]
+
+    def joint_velocity_poses(self, q0: torch.Tensor, action: torch.Tensor, substeps: int):
+        """JointVel_Fk at the fixed base for actions (20,): per-substep geom
+        poses (substeps, G, 3) / (substeps, G, 4) and the final angles (24,)."""
+        pos, rot, (_, q) = self.joint_velocity_fk(self.base[None], q0[None], action[None], substeps)
+        return pos, rot, q[0]
+
     def joint_frames(self, base: torch.Tensor, q: torch.Tensor) -> torch.Tensor:
         """base (..., 4, 4) root-joint body frames, q (..., 24) joint angles ->
         (..., 24, 4, 4) joint frames."""
@@ -482,3 +503,126 @@ class ShadowHand:
         nq = torch.max(torch.min(q[None] + a[None] * k, self.upper), self.lower)
         pos, rot = self.forward_kinematics(nb, nq)
         return pos, rot, (nb[-1], nq[-1])
+
+
+def _scaled(model: HandModel, s: float) -> HandModel:
+    """The model parsed with `scale` s instead of 1 (body and geom positions
+    and geom sizes scale; joint positions do not, as in the parser)."""
+    M, G = model.M.copy(), model.G.copy()
+    M[:, :3, 3] *= s
+    G[:, :3, 3] *= s
+    frames = {}
+    for k, v in model.frames.items():
+        f = v.copy()
+        f[:3, 3] *= s
+        frames[k] = f
+    return HandModel(parent=model.parent.copy(), M=M, p=model.p.copy(), axis=model.axis.copy(),
+                     geom_joint=model.geom_joint.copy(), G=G, geom_type=model.geom_type.copy(),
+                     geom_size=model.geom_size * s, geom_name=list(model.geom_name), frames=frames)
+
+
+HandModel.scaled = _scaled
+
+
+# ------------------------------------------------------------ simulator
+class HandSimulator(MPMSimulator):
+    """Drop-in mirror of mpm/hand.py:68-456 ``HandSimulator``: the MPM
+    simulator (MPMSimulator, batched backend by default) driven by one or two
+    Shadow hands under joint-velocity control.
+
+    The state tuple of env-step boundaries carries the hands' base poses
+    (n_hands, 4, 4) and joint angles (n_hands, 24) after the particle fields
+    and body poses (mpm/hand.py:183-210); set_state runs the kinematics to
+    place the 19 collision primitives of each hand.  compute_forward_kinematics
+    is JointVel_Fk (mpm/hand.py:383-428), so step(action) takes actions of
+    (n_hands, 20) joint velocities, or (n_hands, 26) with a wrist twist.
+
+    models: one HandModel per hand (left before right for two hands, the
+    reference's primitive order), already at the env's scale."""
+
+    def __init__(self, models: Sequence[HandModel], quality: float = 1.0, n_particles: int = 10000,
+                 hand_friction: float = 0.9, action_scale=None, fixed_base: bool = False, device="cuda",
+                 root_frames=None, max_steps: int = 1024, **sim_kwargs):
+        dt = 0.5e-4 / quality
+        dx = 1.0 / (64 * quality)
+        substeps = int(np.ceil(2e-3 / dt))
+        self.models = list(models)
+        self.n_hands = len(self.models)
+        self.device = torch.device(device)
+        self.hands = [ShadowHand(m, device=device, action_scale=action_scale, fixed_base=fixed_base)
+                      for m in self.models]
+        n_bodies = int(sum(m.n_geoms for m in self.models))
+        super().__init__(n_bodies, n_particles=n_particles, dt=dt, dx=dx, substeps=substeps, max_steps=max_steps,
+                         **sim_kwargs)
+        self.n_joints_per_hand = len(JOINTS)
+        self.n_actuators_per_hand = N_ACTUATORS
+        tf, ar = zip(*[h.body_shapes(friction=hand_friction) for h in self.hands])
+        tfsr, args = np.concatenate(tf), np.concatenate(ar)
+        self.init_bodies(tfsr[:, 0], tfsr[:, 2], tfsr[:, 1], tfsr[:, 3], args, None)
+        self.base_pose: List[Optional[torch.Tensor]] = [None] * self.max_steps
+        self.joint_rot: List[Optional[torch.Tensor]] = [None] * self.max_steps
+        rf = (np.stack([default_root_frame(m) for m in self.models]) if root_frames is None
+              else np.asarray(root_frames, np.float64).reshape(self.n_hands, 4, 4))
+        self.base_pose[0] = torch.tensor(rf, dtype=torch.float32, device=self.device)
+        self.joint_rot[0] = torch.tensor(np.tile(DEFAULT_INITIAL_QPOS, (self.n_hands, 1)), dtype=torch.float32,
+                                         device=self.device)
+
+    # ---------------------------------------------------------- kinematics
+    def hand_forward_kinematics(self, base_pose: torch.Tensor, q: torch.Tensor):
+        """mpm/hand.py:347-381: base_pose (S, n_hands, 4, 4), q (S, n_hands,
+        24) -> primitive positions (S, n_bodies, 3) and quaternions (S,
+        n_bodies, 4)."""
+        out = [h.forward_kinematics(base_pose[:, i:i + 1], q[:, i:i + 1]) for i, h in enumerate(self.hands)]
+        return torch.cat([o[0] for o in out], 1), torch.cat([o[1] for o in out], 1)
+
+    def JointVel_Fk(self, f, actions, pos_rot=None):
+        """mpm/hand.py:383-428: per-substep primitive poses of env step f under
+        joint-velocity actions; stores the hands' pose at f + substeps."""
+        base, q = (self.base_pose[f], self.joint_rot[f]) if pos_rot is None else pos_rot
+        actions = torch.as_tensor(np.asarray(actions, np.float32) if not isinstance(actions, torch.Tensor) else actions,
+                                  dtype=torch.float32, device=self.device)
+        assert actions.shape[0] == self.n_hands
+        res = [h.joint_velocity_fk(base[i:i + 1], q[i:i + 1], actions[i:i + 1], self.substeps)
+               for i, h in enumerate(self.hands)]
+        pos = torch.cat([r[0] for r in res], 1)
+        rot = torch.cat([r[1] for r in res], 1)
+        nb = torch.cat([r[2][0] for r in res], 0)
+        nq = torch.cat([r[2][1] for r in res], 0)
+        self.base_pose[f + self.substeps] = nb
+        self.joint_rot[f + self.substeps] = nq
+        return pos, rot, (nb, nq)
+
+    def compute_forward_kinematics(self, f, action, pos_rot=None):
+        return self.JointVel_Fk(f, action, pos_rot=pos_rot)
+
+    def download_pos_rot(self, cur, device):
+        """mpm/hand.py:162-167: the hands' pose of state 0 (later ones reset)."""
+        assert cur == 0
+        for i in range(1, len(self.base_pose)):
+            self.base_pose[i] = self.joint_rot[i] = None
+        return self.base_pose[cur].to(device), self.joint_rot[cur].to(device)
+
+    # -------------------------------------------------------- state tuple
+    def get_state(self, index):
+        """mpm/hand.py:183-187: (x, v, F, C, per-body poses ..., base poses
+        (n_hands, 4, 4), joint angles (n_hands, 24))."""
+        assert index % self.substeps == 0
+        return super().get_state(index) + (self.base_pose[index].detach().cpu().numpy(),
+                                           self.joint_rot[index].detach().cpu().numpy())
+
+    def set_state(self, index, state):
+        """mpm/hand.py:189-210: particles from the tuple, bodies placed by the
+        kinematics of its base poses and joint angles."""
+        assert index % self.substeps == 0
+        self.base_pose[index] = torch.tensor(np.asarray(state[-2]), dtype=torch.float32, device=self.device)
+        self.joint_rot[index] = torch.tensor(np.asarray(state[-1]), dtype=torch.float32, device=self.device)
+        pos, rot = self.hand_forward_kinematics(self.base_pose[index][None], self.joint_rot[index][None])
+        pose = np.concatenate([pos[0].detach().cpu().numpy(), rot[0].detach().cpu().numpy()], 1)
+        super().set_state(index, tuple(np.float32(s) for s in state[:4]) + tuple(pose))
+
+    def step(self, action, pos_rot=None):
+        """mpm/hand.py:437-440: one env step, then the hands' pose at its end
+        becomes the pose of state 0."""
+        super().step(action, pos_rot)
+        self.base_pose[0] = self.base_pose[self.substeps]
+        self.joint_rot[0] = self.joint_rot[self.substeps]
