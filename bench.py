@@ -296,6 +296,11 @@ def run_ours(args, rank, world, local):
     h2d = s0_h.numel() * 4 + poses_pin.numel() * 4
     d2h = g0_h.numel() * 4 + bg_h.numel() * 4 + 4
 
+    # ----- locality: distinct stencil bases per warp of 32 particles, in the
+    # caller's sampling order, right after a sort, and after an env step of
+    # drift (the last checkpoint, never re-sorted)
+    locality = {"sampling_order": bases_per_warp(E, s0), "sorted": bases_per_warp(E, R.stored(0)),
+                f"after_{SUBSTEPS}_substeps": bases_per_warp(E, R.stored(ENV_STEPS))}
     # ----- per-kernel timing (eager, CUDA events on the launching stream)
     kt, cells = kernel_times(E, R, s0, g_final)
     roof = roofline(E, kt, cells)
@@ -307,6 +312,10 @@ def run_ours(args, rank, world, local):
     cpu = None if (args.no_cpu or rank != 0 or world > 1) else cpu_baseline(envs)
     del R, E
     serving = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank, n_req=args.serving_requests)
+    # the same requests arriving three times as fast: above the server's
+    # capacity, so the throughput is the capacity and latency includes queueing
+    serving_sat = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank, n_req=args.serving_requests,
+                                                                         rate_hz=60.0)
     large = None if (args.no_large or world > 1) else large_env_leg(dev)
     rend = None if (args.no_render or world > 1) else render_leg(dev, cpu=not args.no_cpu)
 
@@ -336,6 +345,7 @@ def run_ours(args, rank, world, local):
             "gpu_launches": int(gpu_launches),
             "roofline": roof,
             "kernels_us": {k: round(v, 2) for k, v in kt.items()},
+            "locality": {k: round(v, 2) for k, v in locality.items()},
             "error_word": err,
         }
         if dropin is not None:
@@ -347,12 +357,30 @@ def run_ours(args, rank, world, local):
             out["cpu_baseline"] = cpu
         if serving is not None:
             out["serving"] = serving
+        if serving_sat is not None:
+            out["serving_saturated"] = serving_sat
         if large is not None:
             out["large_env"] = large
         if rend is not None:
             out["render"] = rend
         out["clocks"] = clk.summary()
         print(json.dumps(out))
+
+
+def bases_per_warp(E, state):
+    """Mean number of distinct stencil base cells among 32 consecutive
+    particles of an env (what the warp pre-reduction of the scatters sees)."""
+    x = state[0:3].cpu().numpy()
+    out = []
+    for e, sp in enumerate(E.specs):
+        o = E.p_off[e]
+        b = np.floor(x[:, o:o + sp.n] / sp.dx - 0.5).astype(np.int64)
+        key = (b[0] * 4096 + b[1]) * 4096 + b[2]
+        w = (sp.n // 32) * 32
+        if w:
+            k = np.sort(key[:w].reshape(-1, 32), axis=1)
+            out.append((1 + (np.diff(k, axis=1) != 0).sum(1)).astype(np.float64))
+    return float(np.concatenate(out).mean()) if out else 0.0
 
 
 def kernel_times(E, R, s0, g_final):

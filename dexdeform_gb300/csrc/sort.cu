@@ -21,9 +21,10 @@
 //             scans) -- env e's blocks follow env e-1's, so block bases are
 //             global particle indices;
 //   place  -- perm[base(block) + start(cell) + rank] = old index;
-//   fix    -- per occupied cell: its segment of perm sorted by old index
-//             (the ranks came from atomics in arbitrary order); then the
-//             counts, totals, flags and list are zeroed for the next sort;
+//   fix    -- per occupied block (a warp): each cell's segment of perm put in
+//             increasing old index (the ranks came from atomics in arbitrary
+//             order); then the counts, totals, flags and list are zeroed for
+//             the next sort;
 //   permute -- the 24 state planes gathered into the new order.
 // The caller permutes whatever else is per particle (material, targets) with
 // dexmpm_permute and the same perm.
@@ -183,63 +184,69 @@ __global__ void __launch_bounds__(256) k_sort_place(DexBatch B, DexSortWork W, i
   perm[W.block_base[ci >> 6] + W.cell_start[ci] + W.rank[p]] = p;
 }
 
-// Per occupied cell (a warp per block, two cells per lane): its segment of
-// perm in increasing old index, then the cell count, block total and flag
-// cleared.  A segment of up to kFixSeg entries is sorted in the lane's own
-// row of shared memory (insertion sort; one pass when the input was already
-// in order, as after an env step of drift); a longer one in place in global
-// memory.  The last CTA to finish resets the list count and its own ticket.
-constexpr int kFixSeg = 32;
-constexpr int kFixRow = kFixSeg + 1;  // padded: the lanes' rows start in different banks
+// Per occupied block (one warp): each of its cells' segments of perm put in
+// increasing old index, then the cell counts, block total and flag cleared.
+// The ranks within a cell came from atomics in arbitrary order.  The warp
+// stages a segment of up to kFixMax entries in its shared-memory row, checks
+// whether it is already in order (the usual case after an env step of drift)
+// and otherwise places every entry at its rank -- the number of smaller
+// entries (old indices are distinct) -- each lane counting for every 32nd
+// entry.  Longer segments, which would need more than kFixMax particles in
+// one cell, are insertion-sorted in place by one lane.  The last CTA to
+// finish resets the list count and its own ticket.
+constexpr int kFixMax = 512;
+constexpr int kFixWarps = 8;  // 256-thread CTAs
 __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__restrict__ perm) {
-  __shared__ int32_t rows[256 * kFixRow];
-  const int lane = threadIdx.x & 31;
-  int32_t *row = rows + threadIdx.x * kFixRow;
-  const int warps = gridDim.x * (blockDim.x >> 5);
+  __shared__ int32_t rows[kFixWarps][kFixMax];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int32_t *row = rows[wid];
+  const int warps = gridDim.x * kFixWarps;
   const int cnt = *reinterpret_cast<volatile int32_t *>(W.counters);
-  for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < cnt; item += warps) {
+  for (int item = blockIdx.x * kFixWarps + wid; item < cnt; item += warps) {
     const int blk = W.block_list[item];
     const int base = W.block_base[blk];
+    // lane l owns cells l and l + 32 of the block
+    const int n0 = W.cell_count[(blk << 6) + lane], n1 = W.cell_count[(blk << 6) + 32 + lane];
+    const int st0 = W.cell_start[(blk << 6) + lane], st1 = W.cell_start[(blk << 6) + 32 + lane];
+    unsigned todo[2] = {__ballot_sync(kFull, n0 > 1), __ballot_sync(kFull, n1 > 1)};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int ci = (blk << 6) + 2 * lane + h;
-      const int n = W.cell_count[ci];
-      int32_t *seg = perm + base + W.cell_start[ci];
-      if (n > 1 && n <= kFixSeg) {
-        bool sorted = true;
-        int32_t prev = seg[0];
-        row[0] = prev;
-        for (int a = 1; a < n; ++a) {
-          const int32_t v = seg[a];
-          sorted = sorted && v > prev;
-          prev = v;
-          row[a] = v;
-        }
-        if (!sorted) {
-          for (int a = 1; a < n; ++a) {
-            const int32_t v = row[a];
-            int b = a - 1;
-            while (b >= 0 && row[b] > v) {
-              row[b + 1] = row[b];
-              --b;
+      for (unsigned rest = todo[h]; rest; rest &= rest - 1u) {
+        const int owner = __ffs(rest) - 1;
+        const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
+        int32_t *seg = perm + base + __shfl_sync(kFull, h ? st1 : st0, owner);
+        if (n > kFixMax) {
+          if (lane == 0) {
+            for (int a = 1; a < n; ++a) {
+              const int32_t v = seg[a];
+              int b = a - 1;
+              while (b >= 0 && seg[b] > v) {
+                seg[b + 1] = seg[b];
+                --b;
+              }
+              seg[b + 1] = v;
             }
-            row[b + 1] = v;
           }
-          for (int a = 0; a < n; ++a) seg[a] = row[a];
+          __syncwarp();
+          continue;
         }
-      } else if (n > kFixSeg) {
-        for (int a = 1; a < n; ++a) {
-          const int32_t v = seg[a];
-          int b = a - 1;
-          while (b >= 0 && seg[b] > v) {
-            seg[b + 1] = seg[b];
-            --b;
+        for (int i = lane; i < n; i += 32) row[i] = seg[i];
+        __syncwarp();
+        bool ordered = true;
+        for (int i = lane; i + 1 < n; i += 32) ordered = ordered && row[i] < row[i + 1];
+        if (!__all_sync(kFull, ordered)) {
+          for (int i = lane; i < n; i += 32) {
+            const int32_t v = row[i];
+            int r = 0;
+            for (int j = 0; j < n; ++j) r += row[j] < v;
+            seg[r] = v;
           }
-          seg[b + 1] = v;
         }
+        __syncwarp();
       }
-      W.cell_count[ci] = 0;
     }
+    W.cell_count[(blk << 6) + lane] = 0;
+    W.cell_count[(blk << 6) + 32 + lane] = 0;
     if (lane == 0) {
       W.block_total[blk] = 0;
       W.block_flag[blk] = 0u;

@@ -13,7 +13,8 @@ Forward bar: relative L2 error <= 1e-3 on x, v, F, C after full env steps of
 FP32 state storage between substeps (the reference's storage format).
 Adjoint bar: the gradients of the initial state (x, v, F, C) and of the body
 poses against the oracle's chained substep adjoints (FP32 state storage),
-within max(1e-3, 8 x the oracle's own FP32-vs-FP64-storage difference), from
+within max(1e-3, 8 x the oracle's own FP32-vs-FP64-storage difference, 8 x
+the difference between two GPU runs), from
 a perturbed state (at F = I every singular value is exactly 1 and the
 reference's SVD adjoint multiplies FP32 rounding by its clamped
 1 / (sigma_j^2 - sigma_i^2) = 1e6 factors; away from rest the gradient is
@@ -61,17 +62,30 @@ def _seeded_gradient(E, envs, seed):
     return per_env, E.pack_state(per_env)
 
 
-def _check_adjoint(O, E, R, g0, envs, idx, st0, g_env, T, S):
+def _gradients_twice(E, R, state0, g_final):
+    """Forward + backward twice: the gradients of the first run and the GPU's
+    own run-to-run spread (the float atomics add in a different order)."""
+    out = []
+    for _ in range(2):
+        R.forward(state0)
+        out.append((E.unpack_state(R.backward(g_final).clone()), R.bgrad.cpu().numpy()))
+    assert E.error_word() == 0
+    return out
+
+
+def _check_adjoint(O, E, R, runs, envs, idx, st0, g_env, T, S):
     """The GPU's gradients of the initial state and of the body poses against
-    the oracle's chained adjoint with FP32 state storage.  The bar is the
-    oracle's own sensitivity to that rounding: the distance between its FP32-
-    and FP64-storage gradients, d.  Measured on GB300 over 5-20 substeps of
-    this batch, the GPU sits 1 to 6.4 times d from the FP32-storage oracle
-    (d from 3e-6 to 1.6e-3: contact and yield thresholds that a rounding
-    flips); the test holds it to max(1e-3, 8 d), and the particles whose
-    gradient is off by more than 5% of the field's RMS to under 0.1%."""
-    g0 = E.unpack_state(g0)
-    bg = R.bgrad.cpu().numpy()
+    the oracle's chained adjoint with FP32 state storage.  The bar is set by
+    two rounding sensitivities of the same quantity: d, the distance between
+    the oracle's FP32- and FP64-storage gradients, and e, the distance between
+    two GPU runs (a body-pose gradient sums the contributions of thousands of
+    grid nodes in FP32, in an order the atomics change).  Measured on GB300
+    over 5-20 substeps of this batch, the GPU sits 1 to 6.4 d from the
+    FP32-storage oracle (d from 3e-6 to 1.6e-3: contact and yield thresholds
+    that a rounding flips); the test holds it to max(1e-3, 8 d, 8 e), and the
+    particles whose gradient is off by more than 5% of the field's RMS to
+    under 0.1%."""
+    (g0, bg), (g0b, bgb) = runs
     for e in idx:
         env = envs[e]
         res = {}
@@ -80,16 +94,18 @@ def _check_adjoint(O, E, R, g0, envs, idx, st0, g_env, T, S):
             res[storage] = oracle_chain_adjoint(O, env, [states[t] for t in range(S * T + 1)], g_env[e], "exact")
         (want, bp, br), (w64, bp64, br64) = res["fp32"], res["fp64"]
         for k in ("x", "v", "F", "C"):
-            err, d = rel(g0[e][k], want[k]), rel(want[k], w64[k])
-            assert err < max(1e-3, 8 * d), (env.name, env.n, k, err, d)
+            err, d, n = rel(g0[e][k], want[k]), rel(want[k], w64[k]), rel(g0[e][k], g0b[e][k])
+            assert err < max(1e-3, 8 * d, 8 * n), (env.name, env.n, k, err, d, n)
             dev = np.linalg.norm((g0[e][k] - want[k]).reshape(env.n, -1), axis=1)
             rms = np.sqrt((np.asarray(want[k]).reshape(env.n, -1) ** 2).sum(1).mean())
             assert (dev > 0.05 * rms).mean() < 1e-3, (env.name, k, (dev > 0.05 * rms).mean())
         o = E.body_off[e]
-        for got, w, w2, what in ((bg[:, o:o + env.nb, :3], bp, bp64, "pose position"),
-                                 (bg[:, o:o + env.nb, 4:], br, br64, "pose rotation")):
-            err, d = rel(got, w), rel(w, w2)
-            assert err < max(1e-3, 8 * d), (env.name, what, err, d)
+        for got, other, w, w2, what in ((bg[:, o:o + env.nb, :3], bgb[:, o:o + env.nb, :3], bp, bp64,
+                                         "pose position"),
+                                        (bg[:, o:o + env.nb, 4:], bgb[:, o:o + env.nb, 4:], br, br64,
+                                         "pose rotation")):
+            err, d, n = rel(got, w), rel(w, w2), rel(got, other)
+            assert err < max(1e-3, 8 * d, 8 * n), (env.name, what, err, d, n)
 
 
 def test_batch_config_full_size_forward(cuda, oracle_mod):
@@ -125,10 +141,8 @@ def test_batch_config_full_size_adjoint(cuda, oracle_mod):
     assert R.overlap
     st0 = [W.perturb_state(e, seed=7, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs]
     g_env, g_final = _seeded_gradient(E, envs, 3)
-    R.forward(E.pack_state(st0))
-    g0 = R.backward(g_final).clone()
-    assert E.error_word() == 0
-    _check_adjoint(oracle_mod, E, R, g0, envs, _sampled(envs), st0, g_env, T, S)
+    runs = _gradients_twice(E, R, E.pack_state(st0), g_final)
+    _check_adjoint(oracle_mod, E, R, runs, envs, _sampled(envs), st0, g_env, T, S)
 
 
 def test_large_config_forward(cuda, oracle_mod):
@@ -160,7 +174,5 @@ def test_large_config_adjoint(cuda, oracle_mod):
     assert R.overlap
     st0 = [W.perturb_state(env, seed=8, v_scale=0.1, c_scale=1.0, f_scale=0.02)]
     g_env, g_final = _seeded_gradient(E, [env], 4)
-    R.forward(E.pack_state(st0))
-    g0 = R.backward(g_final).clone()
-    assert E.error_word() == 0
-    _check_adjoint(oracle_mod, E, R, g0, [env], [0], st0, g_env, T, S)
+    runs = _gradients_twice(E, R, E.pack_state(st0), g_final)
+    _check_adjoint(oracle_mod, E, R, runs, [env], [0], st0, g_env, T, S)
