@@ -621,6 +621,7 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, i
     const float inv_m = 1.f / g.w;
     f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
     const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
+    uint32_t hit = 0u;  // bodies whose contact changed this node's velocity
     for (uint32_t rest = near; rest; rest &= rest - 1u) {
       const int b = __ffs(rest) - 1;
       BodyPose cur, nxt;
@@ -628,10 +629,10 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, i
       load_pose(pose, E.body_off + b, cur);
       load_pose(next_pose, E.body_off + b, nxt);
       load_shape(B.body_shape, E.body_off + b, sh);
-      contact_forward(gx, v, cur, nxt, sh, E.dt);
+      if (contact_forward(gx, v, cur, nxt, sh, E.dt)) hit |= 1u << b;
     }
     v = boundary_forward(v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
-    return make_float4(v.x, v.y, v.z, g.w);
+    return make_float4(v.x, v.y, v.z, __uint_as_float(hit));
   };
   auto coords = [](const DexEnv &E, int blk, int &bx, int &by, int &bz) {
     const int local = blk - E.blk_off;
@@ -833,7 +834,8 @@ __global__ void __launch_bounds__(256, DEX_G2P_GRAD_MINB) k_g2p_grad(DexBatch B,
 // ===================================================== grid update adjoint
 // integrator.cu:779-1057 on the blocks of slot X.  The per-body velocities
 // entering each contact are replayed here from (m, mv) instead of being stored
-// by the forward.  Body-pose gradients are reduced in the warp before one
+// by the forward; only the contacts the grid update applied (the bits it left
+// in vout.w) are replayed.  Body-pose gradients are reduced in the warp before one
 // atomic per warp and value.  Every cell of a listed block gets its
 // dL/d(mv, m) written (zero where there is no mass), and dL/dv_out and the
 // slot's grid are zeroed after they are read, so the next use finds them
@@ -847,6 +849,7 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_GRAD_MINB) k_grid_op_grad(Dex
   const bool exact_capsule = (B.flags & DEXMPM_FLAG_EXACT_CAPSULE_GRAD) != 0;
   const int cnt = *reinterpret_cast<volatile int *>(B.block_count + X);
   float4 *grid = reinterpret_cast<float4 *>(slot_grid(B, X));
+  const float4 *vo = reinterpret_cast<const float4 *>(slot_vout(B, X));
   float4 *vgrad = reinterpret_cast<float4 *>(B.vout_grad);
   float4 *igrad = reinterpret_cast<float4 *>(B.in_grad);
   const int32_t *list = slot_list(B, X);
@@ -869,34 +872,33 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_GRAD_MINB) k_grid_op_grad(Dex
     const bool active = in_list && g.w > kMassEps;
     const float inv_m = active ? 1.f / g.w : 0.f;
     const f3 gx = mk3(gxi * E.dx, gyi * E.dx, gzi * E.dx);
-    // forward replay
+    // forward replay of the contacts the grid update applied to this node
+    // (their bodies' bits in vout.w; the others leave the velocity as it is)
     f3 vin[DEXMPM_MAX_BODIES];
     uint32_t touched = 0u;
     f3 v = mk3(g.x * inv_m, g.y * inv_m, g.z * inv_m) + mk3(E.gravity[0], E.gravity[1], E.gravity[2]) * E.dt;
-    const int nbod = in_list ? E.n_bodies : 0;
-    const uint32_t near = bodies_near_block(B, E, pose, bx, by, bz, nbod);
-    if (active) {
-      for (uint32_t rest = near; rest; rest &= rest - 1u) {
-        const int b = __ffs(rest) - 1;
-        BodyPose cur, nxt;
-        BodyShape sh;
-        load_pose(pose, E.body_off + b, cur);
-        load_pose(next_pose, E.body_off + b, nxt);
-        load_shape(B.body_shape, E.body_off + b, sh);
-        f3 before = v;
-        if (contact_forward(gx, v, cur, nxt, sh, E.dt)) {
-          vin[b] = before;
-          touched |= 1u << b;
-        }
+    const uint32_t applied = active ? __float_as_uint(vo[ci].w) : 0u;
+    for (uint32_t rest = applied; rest; rest &= rest - 1u) {
+      const int b = __ffs(rest) - 1;
+      BodyPose cur, nxt;
+      BodyShape sh;
+      load_pose(pose, E.body_off + b, cur);
+      load_pose(next_pose, E.body_off + b, nxt);
+      load_shape(B.body_shape, E.body_off + b, sh);
+      f3 before = v;
+      if (contact_forward(gx, v, cur, nxt, sh, E.dt)) {
+        vin[b] = before;
+        touched |= 1u << b;
       }
     }
     const float4 gv4 = active ? vgrad[ci] : z4;
     f3 gv = boundary_backward(mk3(gv4.x, gv4.y, gv4.z), v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
-    // the warp's lanes share one block, hence one env and one body count
-    for (uint32_t rest = near; rest; rest &= ~(1u << (31 - __clz(rest)))) {
+    // the warp's lanes share one block, hence one env and one body count;
+    // bodies in reverse order of application, any lane's
+    const uint32_t any = __reduce_or_sync(kFull, touched);
+    for (uint32_t rest = any; rest; rest &= ~(1u << (31 - __clz(rest)))) {
       const int b = 31 - __clz(rest);
       const bool hit = (touched >> b) & 1u;
-      if (!__any_sync(kFull, hit)) continue;
       float gc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       float gn[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (hit) {

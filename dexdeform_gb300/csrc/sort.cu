@@ -186,18 +186,31 @@ __global__ void __launch_bounds__(256) k_sort_place(DexBatch B, DexSortWork W, i
 
 // Per occupied block (one warp): each of its cells' segments of perm put in
 // increasing old index, then the cell counts, block total and flag cleared.
-// The ranks within a cell came from atomics in arbitrary order.  The warp
-// stages a segment of up to kFixMax entries in its shared-memory row, checks
-// whether it is already in order (the usual case after an env step of drift)
-// and otherwise places every entry at its rank -- the number of smaller
-// entries (old indices are distinct) -- each lane counting for every 32nd
-// entry.  Longer segments, which would need more than kFixMax particles in
-// one cell, are insertion-sorted in place by one lane.  The last CTA to
-// finish resets the list count and its own ticket.
-constexpr int kFixMax = 512;
+// The ranks within a cell came from atomics in arbitrary order.  The block's
+// entries (contiguous in perm, cell after cell) are staged in the warp's
+// shared-memory row in one coalesced pass; each lane checks whether its two
+// cells are already in order (the usual case after an env step of drift)
+// and the warp then places the entries of each out-of-order cell at their
+// rank -- the number of smaller entries (old indices are distinct) -- each
+// lane counting for every 32nd entry.  A block of more than kFixRow entries
+// is done cell by cell with the same steps; a cell of more than kFixRow is
+// insertion-sorted in place by one lane.  The last CTA to finish resets the
+// list count and its own ticket.
+constexpr int kFixRow = 1024;
 constexpr int kFixWarps = 8;  // 256-thread CTAs
+
+// Ranks of the n entries row[0 .. n) written to seg[rank] (warp-wide).
+__device__ __forceinline__ void place_by_rank(const int32_t *row, int32_t *seg, int n, int lane) {
+  for (int i = lane; i < n; i += 32) {
+    const int32_t v = row[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += row[j] < v;
+    seg[r] = v;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__restrict__ perm) {
-  __shared__ int32_t rows[kFixWarps][kFixMax];
+  __shared__ int32_t rows[kFixWarps][kFixRow];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int32_t *row = rows[wid];
   const int warps = gridDim.x * kFixWarps;
@@ -205,44 +218,57 @@ __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__rest
   for (int item = blockIdx.x * kFixWarps + wid; item < cnt; item += warps) {
     const int blk = W.block_list[item];
     const int base = W.block_base[blk];
+    const int total = W.block_total[blk];
     // lane l owns cells l and l + 32 of the block
     const int n0 = W.cell_count[(blk << 6) + lane], n1 = W.cell_count[(blk << 6) + 32 + lane];
     const int st0 = W.cell_start[(blk << 6) + lane], st1 = W.cell_start[(blk << 6) + 32 + lane];
-    unsigned todo[2] = {__ballot_sync(kFull, n0 > 1), __ballot_sync(kFull, n1 > 1)};
+    if (total <= kFixRow) {
+      for (int i = lane; i < total; i += 32) row[i] = perm[base + i];
+      __syncwarp();
+      bool ok0 = true, ok1 = true;
+      for (int a = 1; a < n0; ++a) ok0 = ok0 && row[st0 + a - 1] < row[st0 + a];
+      for (int a = 1; a < n1; ++a) ok1 = ok1 && row[st1 + a - 1] < row[st1 + a];
+      const unsigned bad[2] = {__ballot_sync(kFull, !ok0), __ballot_sync(kFull, !ok1)};
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      for (unsigned rest = todo[h]; rest; rest &= rest - 1u) {
-        const int owner = __ffs(rest) - 1;
-        const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
-        int32_t *seg = perm + base + __shfl_sync(kFull, h ? st1 : st0, owner);
-        if (n > kFixMax) {
-          if (lane == 0) {
-            for (int a = 1; a < n; ++a) {
-              const int32_t v = seg[a];
-              int b = a - 1;
-              while (b >= 0 && seg[b] > v) {
-                seg[b + 1] = seg[b];
-                --b;
+      for (int h = 0; h < 2; ++h) {
+        for (unsigned rest = bad[h]; rest; rest &= rest - 1u) {
+          const int owner = __ffs(rest) - 1;
+          const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
+          const int st = __shfl_sync(kFull, h ? st1 : st0, owner);
+          place_by_rank(row + st, perm + base + st, n, lane);
+        }
+      }
+      __syncwarp();
+    } else {
+      const unsigned todo[2] = {__ballot_sync(kFull, n0 > 1), __ballot_sync(kFull, n1 > 1)};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        for (unsigned rest = todo[h]; rest; rest &= rest - 1u) {
+          const int owner = __ffs(rest) - 1;
+          const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
+          int32_t *seg = perm + base + __shfl_sync(kFull, h ? st1 : st0, owner);
+          if (n > kFixRow) {
+            if (lane == 0) {
+              for (int a = 1; a < n; ++a) {
+                const int32_t v = seg[a];
+                int b = a - 1;
+                while (b >= 0 && seg[b] > v) {
+                  seg[b + 1] = seg[b];
+                  --b;
+                }
+                seg[b + 1] = v;
               }
-              seg[b + 1] = v;
             }
+            __syncwarp();
+            continue;
           }
+          for (int i = lane; i < n; i += 32) row[i] = seg[i];
           __syncwarp();
-          continue;
+          bool ordered = true;
+          for (int i = lane; i + 1 < n; i += 32) ordered = ordered && row[i] < row[i + 1];
+          if (!__all_sync(kFull, ordered)) place_by_rank(row, seg, n, lane);
+          __syncwarp();
         }
-        for (int i = lane; i < n; i += 32) row[i] = seg[i];
-        __syncwarp();
-        bool ordered = true;
-        for (int i = lane; i + 1 < n; i += 32) ordered = ordered && row[i] < row[i + 1];
-        if (!__all_sync(kFull, ordered)) {
-          for (int i = lane; i < n; i += 32) {
-            const int32_t v = row[i];
-            int r = 0;
-            for (int j = 0; j < n; ++j) r += row[j] < v;
-            seg[r] = v;
-          }
-        }
-        __syncwarp();
       }
     }
     W.cell_count[(blk << 6) + lane] = 0;

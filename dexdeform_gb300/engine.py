@@ -169,11 +169,12 @@ class BatchEngine:
         self.body_shape = torch.tensor(shapes, **f32)
         cells = self.n_blocks * 64
         self.n_grid_slots = K = max(2, int(grid_slots))
-        self.grid = torch.zeros((K, cells, 4), **f32)
-        self.vout = torch.zeros((K, cells, 4), **f32)
-        self.vout_grad = torch.zeros((cells, 4), **f32) if grad else None
-        self.in_grad = torch.zeros((cells, 4), **f32) if grad else None
-        self.block_flag = torch.zeros((K, self.n_blocks), **i32)
+        # grids, gradient grids and flags are zeroed by dexmpm_reset below
+        self.grid = torch.empty((K, cells, 4), **f32)
+        self.vout = torch.empty((K, cells, 4), **f32)
+        self.vout_grad = torch.empty((cells, 4), **f32) if grad else None
+        self.in_grad = torch.empty((cells, 4), **f32) if grad else None
+        self.block_flag = torch.empty((K, self.n_blocks), **i32)
         self.block_list = torch.zeros((K, self.n_blocks), **i32)
         self.block_count = torch.zeros(K, **i32)
         self.done_counter = torch.zeros(1, **i32)

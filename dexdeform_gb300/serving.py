@@ -93,6 +93,7 @@ class _Batch:
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
         self.use_graphs = use_graphs
         self.graphs = {}
+        self.uses = {}
 
     def _forward(self):
         self.E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses)
@@ -107,9 +108,13 @@ class _Batch:
 
     def run(self, kind: str) -> bool:
         """Run the round's launch sequence; True when it was captured as a
-        new CUDA graph (first use of this membership and kind)."""
+        new CUDA graph.  A membership's first round of a kind runs eagerly
+        and its second is captured (many memberships last one round while
+        requests arrive and leave), later ones replay the graph."""
+        self.uses[kind] = self.uses.get(kind, 0) + 1
         before = len(self.graphs)
-        run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward, self.use_graphs)
+        run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward,
+                  self.use_graphs and self.uses[kind] > 1)
         return len(self.graphs) > before
 
 

@@ -161,7 +161,9 @@ int render(float *sdf_volume, float *box_min, float *box_max, float *color_volum
  *   slot ((x&3)*16 + (y&3)*4 + (z&3)).  Cell values are float4.
  * Grid slots: `n_slots` copies of
  *     grid   (m v.x, m v.y, m v.z, m) after P2G
- *     vout   (v.x, v.y, v.z, m) after the grid update
+ *     vout   (v.x, v.y, v.z, c) after the grid update; c holds, as uint32
+ *            bits, the env's bodies whose contact changed the node (bit b:
+ *            body b), which the grid adjoint replays
  *   with a block flag array, an active-block list and its count per slot.
  *   P2G into slot k appends the blocks its stencils touch to slot k's list.
  *   Forward substeps alternate two slots; each grid update clears the slot of
