@@ -262,13 +262,17 @@ class BatchEngine:
         self.launches += 1
 
     # ----------------------------------------------------------- state I/O
-    def new_slots(self, n: int) -> torch.Tensor:
-        return torch.zeros((n, N.STATE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
+    def new_slots(self, n: int, zero: bool = True) -> torch.Tensor:
+        """n state slots; zero=False leaves them uninitialised (for slots every
+        particle's planes are written into before they are read)."""
+        f = torch.zeros if zero else torch.empty
+        return f((n, N.STATE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
 
-    def new_tape(self, n: int) -> torch.Tensor:
+    def new_tape(self, n: int, zero: bool = True) -> torch.Tensor:
         """n tape slots (the per-particle SVD and stress a recomputed forward
         P2G stores for its adjoint)."""
-        return torch.zeros((n, TAPE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
+        f = torch.zeros if zero else torch.empty
+        return f((n, TAPE_PLANES, self.n_particles), dtype=torch.float32, device=self.device)
 
     def pack_state(self, per_env: Sequence[dict]) -> torch.Tensor:
         """Host dicts (x, v (n,3); F, C (n,3,3)) -> one device slot (24, Np)."""

@@ -85,11 +85,13 @@ class _Batch:
                              grid_slots=substeps + 2 if grad else 2)
         self.T = substeps
         nb = max(self.E.n_bodies, 1)
-        self.slot = self.E.new_slots(self.T + 1)
+        # slot 0 and the gradient are gathered into and the kernels write the
+        # rest before reading them: no zero fill
+        self.slot = self.E.new_slots(self.T + 1, zero=False)
         self.poses = torch.zeros((self.T + 1, nb, 8), device=device)
         if grad:
-            self.gbuf = self.E.new_slots(2)
-            self.tape = self.E.new_tape(self.T)
+            self.gbuf = self.E.new_slots(2, zero=False)
+            self.tape = self.E.new_tape(self.T, zero=False)
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
         self.use_graphs = use_graphs
         self.graphs = {}
