@@ -90,12 +90,45 @@ def footprint_bytes(specs: Sequence[EnvSpec], n_slots: int = 2, grad: bool = Fal
     return int(b)
 
 
+@dataclass(frozen=True)
+class Capacity:
+    """Table sizes a BatchEngine is built for: particles per state plane, 4^3
+    grid blocks per grid slot (the slots' stride), bodies, particle tiles and
+    envs.  An engine re-laid out for another set of envs (BatchEngine.relayout)
+    keeps its buffers while the new layout fits."""
+    particles: int = 0
+    blocks: int = 0
+    bodies: int = 0
+    tiles: int = 0
+    envs: int = 0
+
+    @classmethod
+    def of(cls, specs: Sequence[EnvSpec], tile_size: int) -> "Capacity":
+        n = blk = nb = tiles = 0
+        for s in specs:
+            n += s.n
+            blk += (s.grid_dim[0] // 4) * (s.grid_dim[1] // 4) * (s.grid_dim[2] // 4)
+            nb += s.nb
+            tiles += -(-s.n // tile_size)
+        return cls(particles=n, blocks=blk, bodies=nb, tiles=tiles, envs=len(specs))
+
+    def holds(self, other: "Capacity") -> bool:
+        return all(getattr(self, k) >= getattr(other, k) for k in self.__dataclass_fields__)
+
+    def union(self, other: "Capacity") -> "Capacity":
+        return Capacity(**{k: max(getattr(self, k), getattr(other, k)) for k in self.__dataclass_fields__})
+
+    def scaled(self, factor: float) -> "Capacity":
+        return Capacity(**{k: int(math.ceil(getattr(self, k) * factor)) for k in self.__dataclass_fields__})
+
+
 def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
     """Host-side layout of a batch: particle / block / body offsets per env,
-    particle tiles (env, first particle) that never straddle envs, the owning
-    env of every grid block, and the DexEnv descriptors."""
+    particle tiles (env, first particle) that never straddle envs, as an
+    (n_tiles, 2) int32 array, the owning env of every grid block (int32), and
+    the DexEnv descriptors."""
     envs = (N.DexEnv * len(specs))()
-    tiles, block_env, p_off, blk_off, body_off = [], [], [], [], []
+    p_off, blk_off, body_off, tiles, nblk = [], [], [], [], []
     p = blk = body = 0
     for e, s in enumerate(specs):
         nbx, nby, nbz = (g // 4 for g in s.grid_dim)
@@ -109,11 +142,14 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
         p_off.append(p)
         blk_off.append(blk)
         body_off.append(body)
-        tiles += [(e, t) for t in range(0, s.n, tile_size)]
-        block_env += [e] * (nbx * nby * nbz)
+        first = np.arange(0, s.n, tile_size, dtype=np.int32)
+        tiles.append(np.stack([np.full_like(first, e), first], 1))
+        nblk.append(nbx * nby * nbz)
         p += s.n
         blk += nbx * nby * nbz
         body += s.nb
+    tiles = np.concatenate(tiles) if tiles else np.zeros((0, 2), np.int32)
+    block_env = np.repeat(np.arange(len(specs), dtype=np.int32), nblk)
     return dict(envs=envs, tiles=tiles, block_env=block_env, p_off=p_off, blk_off=blk_off, body_off=body_off,
                 n_blocks=blk, n_bodies=body, n_particles=p)
 
@@ -121,52 +157,44 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
 class BatchEngine:
     def __init__(self, specs: Sequence[EnvSpec], device="cuda", tile_size: int = 128,
                  grid_ctas: Optional[int] = None, n_slots: int = 2, grad: bool = False,
-                 capsule_grad: str = "reference", grid_slots: int = 2, stride: int = 0):
+                 capsule_grad: str = "reference", grid_slots: int = 2, stride: int = 0,
+                 capacity: Optional[Capacity] = None):
         """grid_slots: 2 for forward use; 2 + T lets Rollout / DiffSim keep the
         grids of a recomputed env step of T substeps for the adjoint.
         capsule_grad: "reference" drops the capsule-normal term of the body
         pose gradient as the reference does; "exact" keeps it.  stride: at
         least this many entries per state plane (the planes of a caller's
-        storage sized for more particles than the envs hold now)."""
+        storage sized for more particles than the envs hold now).  capacity:
+        size the tables and grid slots for at least this much, so that
+        relayout can later move the engine to other envs without new
+        buffers."""
         N.require_cuda()
         self.lib = N.load()
         self.device = torch.device(device)
-        self.specs = list(specs)
         self.tile_size = int(tile_size)
         assert self.tile_size in (64, 128, 256)
         self.grad = grad
-        for s in self.specs:
-            assert all(g % 4 == 0 and g >= 8 for g in s.grid_dim), "grid dims must be multiples of 4"
-            if s.nb > N.MAX_BODIES:
-                raise N.DexError(f"{s.nb} bodies > {N.MAX_BODIES} per env")
-        n_real = max(sum(s.n for s in self.specs), int(stride))
+        self._check_specs(specs)
+        need = Capacity.of(specs, self.tile_size)
+        cap = need if capacity is None else need.union(capacity)
+        n_real = max(cap.particles, int(stride))
         self.n_particles = max(32, ((n_real + 31) // 32) * 32)
-        L = plan_layout(self.specs, self.tile_size)
-        self.p_off, self.blk_off, self.body_off = L["p_off"], L["blk_off"], L["body_off"]
-        envs, tiles, block_env = L["envs"], L["tiles"], L["block_env"]
-        self.n_blocks, self.n_bodies = L["n_blocks"], L["n_bodies"]
+        self.capacity = Capacity(particles=self.n_particles, blocks=max(cap.blocks, 1), bodies=max(cap.bodies, 1),
+                                 tiles=max(cap.tiles, 1), envs=max(cap.envs, 1))
+        # grid slots hold capacity.blocks blocks each (their stride), whatever
+        # the current layout uses
+        self.n_blocks = self.capacity.blocks
         dev = self.device
         f32 = dict(dtype=torch.float32, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
-        self.envs_t = torch.frombuffer(bytearray(bytes(envs)), dtype=torch.uint8).to(dev)
-        self.tiles_t = torch.tensor(np.asarray(tiles, np.int32).reshape(-1, 2) if tiles else np.zeros((0, 2), np.int32),
-                                    **i32)
-        self.block_env_t = torch.tensor(np.asarray(block_env, np.int32), **i32)
-        Np = self.n_particles
+        C, Np = self.capacity, self.n_particles
+        self.envs_t = torch.zeros(C.envs * ctypes.sizeof(N.DexEnv), dtype=torch.uint8, device=dev)
+        self.tiles_t = torch.zeros((C.tiles, 2), **i32)
+        self.block_env_t = torch.zeros(C.blocks, **i32)
         # material planes: mass, vol, mu, lambda, yield stress
-        mat = np.zeros((MATERIAL_PLANES, Np), np.float32)
-        shapes = np.zeros((max(self.n_bodies, 1), 8), np.float32)
-        for e, s in enumerate(self.specs):
-            o = self.p_off[e]
-            mat[0, o:o + s.n] = s.mass
-            mat[1, o:o + s.n] = s.vol
-            mat[2:5, o:o + s.n] = np.asarray(s.mu_lam_yield, np.float32).T
-            if s.nb:
-                shapes[self.body_off[e]:self.body_off[e] + s.nb, :4] = s.body_tfsr
-                shapes[self.body_off[e]:self.body_off[e] + s.nb, 4:] = s.body_args
-        self.mat = torch.tensor(mat, **f32)
+        self.mat = torch.zeros((MATERIAL_PLANES, self.n_particles), **f32)
         self.mass, self.vol, self.mly = self.mat[0], self.mat[1], self.mat[2:5]
-        self.body_shape = torch.tensor(shapes, **f32)
+        self.body_shape = torch.zeros((C.bodies, 8), **f32)
         cells = self.n_blocks * 64
         self.n_grid_slots = K = max(2, int(grid_slots))
         # grids, gradient grids and flags are zeroed by dexmpm_reset below
@@ -182,8 +210,8 @@ class BatchEngine:
         self.states = torch.zeros((n_slots, N.STATE_PLANES, Np), **f32)
         self.grid_ctas = int(grid_ctas or sm_count(self.device) * 4)
         b = N.DexBatch()
-        b.n_envs, b.n_particles, b.n_tiles, b.n_blocks = len(self.specs), Np, len(tiles), self.n_blocks
-        b.n_bodies, b.tile_size, b.grid_ctas = self.n_bodies, self.tile_size, self.grid_ctas
+        b.n_particles, b.n_blocks = Np, self.n_blocks
+        b.tile_size, b.grid_ctas = self.tile_size, self.grid_ctas
         assert capsule_grad in ("reference", "exact")
         b.flags = N.FLAG_EXACT_CAPSULE_GRAD if capsule_grad == "exact" else 0
         b.n_slots = K
@@ -200,7 +228,75 @@ class BatchEngine:
         self.fslot = 0          # grid slot of the next forward substep (0 or 1)
         self.launches = 0
         self._sortw = None      # scratch of the particle sort, allocated on first use
+        self._write_layout(specs, material=True, staged=False)
         N.check(self.lib.dexmpm_reset(self._bp, N.stream_ptr()), "dexmpm_reset")
+
+    @staticmethod
+    def _check_specs(specs):
+        for s in specs:
+            assert all(g % 4 == 0 and g >= 8 for g in s.grid_dim), "grid dims must be multiples of 4"
+            if s.nb > N.MAX_BODIES:
+                raise N.DexError(f"{s.nb} bodies > {N.MAX_BODIES} per env")
+
+    def _upload(self, dst: torch.Tensor, src: np.ndarray, staged: bool):
+        t = torch.from_numpy(np.require(src, requirements=["C", "W"]))
+        if staged:
+            # through pinned memory, ordered on the current stream: the host
+            # does not wait for the device work queued ahead of the copy
+            dst.copy_(t.pin_memory(), non_blocking=True)
+        else:
+            dst.copy_(t)
+
+    def _write_layout(self, specs, material: bool, staged: bool):
+        L = plan_layout(specs, self.tile_size)
+        self.specs = list(specs)
+        self.p_off, self.blk_off, self.body_off = L["p_off"], L["blk_off"], L["body_off"]
+        self.n_bodies, self.used_blocks = L["n_bodies"], L["n_blocks"]
+        tiles = L["tiles"]
+        if len(specs):
+            self._upload(self.envs_t[:ctypes.sizeof(N.DexEnv) * len(specs)],
+                         np.frombuffer(bytes(L["envs"]), np.uint8), staged)
+        if len(tiles):
+            self._upload(self.tiles_t[:len(tiles)], tiles, staged)
+        if L["n_blocks"]:
+            self._upload(self.block_env_t[:L["n_blocks"]], L["block_env"], staged)
+        if self.n_bodies:
+            shapes = np.zeros((self.n_bodies, 8), np.float32)
+            for e, s in enumerate(self.specs):
+                if s.nb:
+                    shapes[self.body_off[e]:self.body_off[e] + s.nb, :4] = s.body_tfsr
+                    shapes[self.body_off[e]:self.body_off[e] + s.nb, 4:] = s.body_args
+            self._upload(self.body_shape[:self.n_bodies], shapes, staged)
+        if material:
+            mat = np.zeros((MATERIAL_PLANES, L["n_particles"]), np.float32)
+            for e, s in enumerate(self.specs):
+                o = self.p_off[e]
+                mat[0, o:o + s.n] = s.mass
+                mat[1, o:o + s.n] = s.vol
+                mat[2:5, o:o + s.n] = np.asarray(s.mu_lam_yield, np.float32).T
+            if L["n_particles"]:
+                self._upload(self.mat[:, :L["n_particles"]], mat, staged)
+        b = self.batch
+        b.n_envs, b.n_tiles, b.n_bodies = len(self.specs), len(tiles), self.n_bodies
+
+    def fits(self, specs: Sequence[EnvSpec]) -> bool:
+        """True when relayout(specs) can keep this engine's buffers."""
+        return self.capacity.holds(Capacity.of(specs, self.tile_size))
+
+    def relayout(self, specs: Sequence[EnvSpec], material: bool = True):
+        """Move the engine to another set of envs within its capacity: rewrite
+        the env, tile and block tables, the body shapes and (material=True)
+        the material planes, on the current stream through pinned staging, so
+        that the host does not wait.  The grid slots stay: every slot's active
+        blocks are cleared by the launch that consumes it, so a slot left in
+        use by the last forward substep is still cleared by the next one.
+        CUDA graphs captured before this call hold the old launch shapes and
+        must not be replayed after it.  With material=False the caller writes
+        mass, vol, mu, lambda, yield stress into mat itself."""
+        self._check_specs(specs)
+        if not self.fits(specs):
+            raise N.DexError(f"layout of {len(specs)} envs exceeds the engine's capacity {self.capacity}")
+        self._write_layout(specs, material=material, staged=self.device.type == "cuda")
 
     # ------------------------------------------------------------ material
     def use_material(self, mat: Optional[torch.Tensor] = None):
@@ -430,11 +526,13 @@ class BatchEngine:
         """Change the particle tile size and the persistent grid-kernel CTA
         count (launch shape only; no buffer changes)."""
         assert tile_size in (64, 128, 256) and grid_ctas > 0
-        L = plan_layout(self.specs, tile_size)
-        tiles = L["tiles"]
+        tiles = plan_layout(self.specs, tile_size)["tiles"]
         self.tile_size, self.grid_ctas = int(tile_size), int(grid_ctas)
-        self.tiles_t = torch.tensor(np.asarray(tiles, np.int32).reshape(-1, 2) if tiles else
-                                    np.zeros((0, 2), np.int32), dtype=torch.int32, device=self.device)
+        if len(tiles) > self.tiles_t.shape[0]:
+            self.tiles_t = torch.zeros((len(tiles), 2), dtype=torch.int32, device=self.device)
+            self.capacity = Capacity(**{**self.capacity.__dict__, "tiles": len(tiles)})
+        if len(tiles):
+            self.tiles_t[:len(tiles)].copy_(torch.from_numpy(tiles))
         b = self.batch
         b.tiles, b.n_tiles, b.tile_size, b.grid_ctas = self.tiles_t.data_ptr(), len(tiles), self.tile_size, \
             self.grid_ctas

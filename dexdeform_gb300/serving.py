@@ -16,8 +16,12 @@ running requests together one env step (``substeps`` substeps) per round:
 
 Membership changes at round boundaries (a request that arrives while others
 run joins at the next round; a finished request leaves and frees its memory).
-Engines and their CUDA graphs are cached per membership.  Results do not depend
-on co-scheduling: envs never interact, and a request computes the same
+Each phase has one engine sized to a capacity: a membership change re-lays it
+out in place (new env, tile and block tables, material and body shapes copied
+on the stream, no new buffers, no host wait); it is rebuilt, larger, only when
+a membership outgrows it.  A membership that stays for `capture_after` rounds
+is captured as a CUDA graph and replayed while it lasts.  Results do not
+depend on co-scheduling: envs never interact, and a request computes the same
 substeps in the same order alone or in the mix.
 """
 from __future__ import annotations
@@ -31,7 +35,7 @@ from typing import Dict, List, Optional
 import numpy as np
 import torch
 
-from .engine import BatchEngine, EnvSpec, footprint_bytes, pack_poses, run_graph
+from .engine import BatchEngine, Capacity, EnvSpec, footprint_bytes, pack_poses, run_graph
 
 
 @dataclass
@@ -69,6 +73,9 @@ class _Resident:
         buf[0:3], buf[3:6] = st["x"].T, st["v"].T
         buf[6:15], buf[15:24] = st["F"].reshape(env.n, 9).T, st["C"].reshape(env.n, 9).T
         self.state = torch.tensor(buf, **f)
+        mat = np.zeros((5, env.n), np.float32)
+        mat[0], mat[1], mat[2:5] = env.mass, env.vol, np.asarray(env.mu_lam_yield, np.float32).T
+        self.mat = torch.tensor(mat, **f)   # mass, vol, mu, lambda, yield stress
         n_sub = req.horizon * substeps
         self.poses = torch.tensor(pack_poses(env.poses[:n_sub + 1, :, :3], env.poses[:n_sub + 1, :, 3:]), **f)
         self.ckpt = [self.state.clone()] if req.grad else None
@@ -76,15 +83,17 @@ class _Resident:
         self.bgrad = torch.zeros_like(self.poses) if req.grad else None
 
 
-class _Batch:
-    """A BatchEngine for one membership plus its per-round graphs."""
+class _Arena:
+    """One phase's BatchEngine (forward, or adjoint with kept grid slots) with
+    its round buffers, sized to a capacity and re-laid out for each new
+    membership, plus the CUDA graphs of the current membership."""
 
-    def __init__(self, reqs: List[Request], substeps: int, grad: bool, device, tile_size: int, use_graphs: bool):
-        self.ids = tuple(r.rid for r in reqs)
-        self.E = BatchEngine([r.spec for r in reqs], device=device, grad=grad, tile_size=tile_size,
-                             grid_slots=substeps + 2 if grad else 2)
+    def __init__(self, capacity: Capacity, substeps: int, grad: bool, device, tile_size: int, use_graphs: bool,
+                 capture_after: int):
+        self.E = BatchEngine([], device=device, grad=grad, tile_size=tile_size,
+                             grid_slots=substeps + 2 if grad else 2, capacity=capacity)
         self.T = substeps
-        nb = max(self.E.n_bodies, 1)
+        nb = self.E.capacity.bodies
         # slot 0 and the gradient are gathered into and the kernels write the
         # rest before reading them: no zero fill
         self.slot = self.E.new_slots(self.T + 1, zero=False)
@@ -94,8 +103,26 @@ class _Batch:
             self.tape = self.E.new_tape(self.T, zero=False)
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
         self.use_graphs = use_graphs
+        self.capture_after = max(1, int(capture_after))
+        self.key = None
         self.graphs = {}
         self.uses = {}
+
+    def assign(self, reqs: List[Request], resident: Dict[int, "_Resident"]) -> bool:
+        """Lay the engine out for these requests (True when that changed the
+        layout); the material planes are copied from the residents."""
+        key = tuple(r.rid for r in reqs)
+        if key == self.key:
+            return False
+        E = self.E
+        E.relayout([r.spec for r in reqs], material=False)
+        for e, r in enumerate(reqs):
+            o = E.p_off[e]
+            E.mat[:, o:o + r.env.n].copy_(resident[r.rid].mat)
+        self.key = key
+        self.graphs.clear()
+        self.uses.clear()
+        return True
 
     def _forward(self):
         self.E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses)
@@ -110,13 +137,13 @@ class _Batch:
 
     def run(self, kind: str) -> bool:
         """Run the round's launch sequence; True when it was captured as a
-        new CUDA graph.  A membership's first round of a kind runs eagerly
-        and its second is captured (many memberships last one round while
-        requests arrive and leave), later ones replay the graph."""
+        new CUDA graph.  A membership's rounds run eagerly until its
+        capture_after-th, which is captured (many memberships last a round or
+        two while requests arrive and leave); later ones replay the graph."""
         self.uses[kind] = self.uses.get(kind, 0) + 1
         before = len(self.graphs)
         run_graph(self.E, self.graphs, kind, self._forward if kind == "fwd" else self._backward,
-                  self.use_graphs and self.uses[kind] > 1)
+                  self.use_graphs and self.uses[kind] >= self.capture_after)
         return len(self.graphs) > before
 
 
@@ -124,7 +151,7 @@ class Server:
     """Continuous-batching MPM server on one GPU."""
 
     def __init__(self, substeps=50, hbm_budget_bytes=180 * 2 ** 30, device="cuda", tile_size=128,
-                 use_graphs=True, max_cached_batches=8, max_inflight_rounds=3):
+                 use_graphs=True, max_inflight_rounds=3, capture_after=3, growth=1.25):
         self.T = substeps
         self.budget = int(hbm_budget_bytes)
         self.device = torch.device(device)
@@ -135,8 +162,11 @@ class Server:
         self.resident: Dict[int, _Resident] = {}
         self.done: List[Request] = []
         self.in_use = 0
-        self.cache: "collections.OrderedDict[tuple, _Batch]" = collections.OrderedDict()
-        self.max_cached = max_cached_batches
+        # one engine per phase (False: forward, True: adjoint), grown by
+        # `growth` beyond the membership that outgrew it
+        self.arenas: Dict[bool, _Arena] = {}
+        self.capture_after = capture_after
+        self.growth = float(growth)
         self.s_fwd = torch.cuda.Stream(device=self.device)
         self.s_bwd = torch.cuda.Stream(device=self.device)
         self.rounds = 0
@@ -147,11 +177,13 @@ class Server:
         self.max_inflight = max(1, int(max_inflight_rounds))
         self._round_reqs: List[Request] = []
         self._round_batches: list = []
-        # where the time goes: engines built and graphs captured (host
-        # seconds), and per round the device time of the state gathers, the
-        # substeps and the scatters on each stream (CUDA events, read at the
-        # end of run)
+        # where the time goes: engines built, re-laid out and graphs captured
+        # (host seconds), and per round the device time of the state gathers,
+        # the substeps and the scatters on each stream (CUDA events, read at
+        # the end of run)
         self.engine_builds = 0
+        self.relayouts = 0
+        self.host_relayout_s = 0.0
         self.graph_captures = 0
         self.host_build_s = 0.0
         self.host_capture_s = 0.0
@@ -180,19 +212,22 @@ class Server:
             self.resident[r.rid] = _Resident(r, self.T, self.device)
 
     def _batch(self, reqs, grad):
-        key = (grad,) + tuple(r.rid for r in reqs)
-        b = self.cache.get(key)
-        if b is None:
+        a = self.arenas.get(grad)
+        need = Capacity.of([r.spec for r in reqs], self.tile_size)
+        if a is None or not a.E.capacity.holds(need):
             t0 = time.perf_counter()
-            b = _Batch(reqs, self.T, grad, self.device, self.tile_size, self.use_graphs)
+            cap = need.scaled(self.growth)
+            if a is not None:
+                cap = cap.union(a.E.capacity)
+            a = _Arena(cap, self.T, grad, self.device, self.tile_size, self.use_graphs, self.capture_after)
+            self.arenas[grad] = a
             self.engine_builds += 1
             self.host_build_s += time.perf_counter() - t0
-            self.cache[key] = b
-            while len(self.cache) > self.max_cached:
-                self.cache.popitem(last=False)
-        else:
-            self.cache.move_to_end(key)
-        return b
+        t0 = time.perf_counter()
+        if a.assign(reqs, self.resident):
+            self.relayouts += 1
+            self.host_relayout_s += time.perf_counter() - t0
+        return a
 
     # -------------------------------------------------------------- round
     def _mark(self):
@@ -359,9 +394,10 @@ class Server:
         """Where the serving time went (call after run): device seconds of the
         state gathers, the substeps and the scatters per stream, their busy
         fraction of the wall time, and the host time spent building engines
-        and capturing graphs for new memberships."""
+        building engines, re-laying them out and capturing graphs."""
         out = {"wall_s": round(wall_s, 3), "rounds": self.rounds, "engine_builds": self.engine_builds,
-               "graph_captures": self.graph_captures, "host_build_s": round(self.host_build_s, 3),
+               "relayouts": self.relayouts, "graph_captures": self.graph_captures,
+               "host_build_s": round(self.host_build_s, 3), "host_relayout_s": round(self.host_relayout_s, 3),
                "host_capture_s": round(self.host_capture_s, 3)}
         for kind in ("fwd", "bwd"):
             g = c = sc = 0.0

@@ -255,6 +255,30 @@ def test_layout_plan_and_footprint():
     assert 0 < a < b
 
 
+def test_capacity_covers_the_layout_it_is_computed_from():
+    """Capacity.of counts what plan_layout lays out (particles, blocks,
+    bodies, tiles, envs), and a capacity holds a layout exactly when every
+    count fits: what BatchEngine.relayout checks before it keeps its buffers."""
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import Capacity, EnvSpec, plan_layout
+    envs = W.batch_envs(3, n_envs=6, steps=2, n_lo=100, n_hi=900)
+    specs = [EnvSpec.from_env(e) for e in envs]
+    for tile in (64, 128, 256):
+        L = plan_layout(specs, tile)
+        c = Capacity.of(specs, tile)
+        assert (c.particles, c.blocks, c.bodies, c.tiles, c.envs) == (
+            L["n_particles"], L["n_blocks"], L["n_bodies"], len(L["tiles"]), len(specs))
+    c = Capacity.of(specs, 128)
+    part = Capacity.of(specs[:3], 128)
+    assert c.holds(part) and not part.holds(c) and c.holds(c)
+    assert c.union(part) == c and part.union(c) == c
+    g = part.scaled(1.25)
+    assert g.holds(part) and g.blocks == -(-part.blocks * 5 // 4)
+    # one count over is enough to not fit
+    assert not c.holds(Capacity(**{**c.__dict__, "bodies": c.bodies + 1}))
+    assert Capacity.of([], 128) == Capacity()
+
+
 def test_workloads_are_seeded_and_in_range():
     from dexdeform_gb300 import workloads as W
     a, b = W.batch_envs(0, n_envs=16, steps=5), W.batch_envs(0, n_envs=16, steps=5)

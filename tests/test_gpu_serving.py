@@ -45,6 +45,77 @@ def test_mixed_results_equal_alone(cuda):
             assert rel(b, a) < (1e-5 if k == "state" else 5e-4), (r.rid, k)
 
 
+def _run(E, envs, T, grad):
+    """T substeps forward (and with grad the adjoint of a fixed final
+    gradient) of envs on engine E; returns the final state (and the state-0
+    and body-pose gradients)."""
+    s0 = E.pack_state([_state(e) for e in envs])
+    sts = E.new_slots(T + 1)
+    sts[0].copy_(s0)
+    poses = torch.tensor(E.pack_poses([e.poses[:T + 1, :, :3] for e in envs],
+                                      [e.poses[:T + 1, :, 3:] for e in envs]), device="cuda")
+    if not grad:
+        E.run_substeps(list(sts), poses)
+        return (sts[T].clone(),)
+    tape = E.new_tape(T)
+    E.run_substeps(list(sts), poses, kept=True, tapes=tape)
+    g = torch.zeros_like(s0)
+    g[0:6] = 1.0
+    scratch = torch.zeros_like(s0)
+    bgrad = torch.zeros_like(poses)
+    out = E.run_adjoint(list(sts), g, scratch, poses, bgrad, tapes=tape)
+    return sts[T].clone(), out.clone(), bgrad.clone()
+
+
+def _state(env):
+    from dexdeform_gb300 import workloads as W
+    return W.perturb_state(env, seed=5, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+
+
+@pytest.mark.parametrize("grad", [False, True])
+def test_relayout_equals_fresh_engine(cuda, grad):
+    """An engine re-laid out in place (another number of envs, other grid
+    sizes and bodies; a forward slot left in use by the previous layout)
+    computes what an engine built for the new envs does, within the bars of
+    the other schedule-equivalence tests (the float atomics add in another
+    order in each run): states 2e-4, gradients 5e-4."""
+    from dexdeform_gb300 import _native as N
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.engine import BatchEngine, Capacity, EnvSpec
+    T = 8
+    A = W.batch_envs(1, n_envs=4, steps=T, n_lo=500, n_hi=3000, sort=False)
+    B = W.batch_envs(2, n_envs=3, steps=T, n_lo=500, n_hi=3000, sort=False)
+    spec = lambda envs: [EnvSpec.from_env(e) for e in envs]
+    cap = Capacity.of(spec(A), 128).union(Capacity.of(spec(B), 128))
+    kw = dict(grad=grad, grid_slots=T + 2 if grad else 2, capacity=cap)
+    arena = BatchEngine(spec(A), **kw)
+    _run(arena, A, T, grad)
+    for envs in (B, A[1:3], A):
+        arena.relayout(spec(envs))
+        got = _run(arena, envs, T, grad)
+        want = _run(BatchEngine(spec(envs), **kw), envs, T, grad)
+        assert arena.error_word() == 0
+        for (a, b), tol in zip(zip(got, want), (2e-4, 5e-4, 5e-4)):
+            assert rel(a.cpu().numpy(), b.cpu().numpy()) < tol
+    big = W.batch_envs(3, n_envs=6, steps=T, n_lo=500, n_hi=3000, sort=False)
+    assert not arena.fits(spec(big))
+    with pytest.raises(N.DexError):
+        arena.relayout(spec(big))
+
+
+def test_serving_relays_out_instead_of_rebuilding(cuda):
+    """Membership changes re-lay the phase's engine out; it is rebuilt only
+    when a membership outgrows it."""
+    from dexdeform_gb300.serving import Server
+    T = 10
+    srv = Server(substeps=T, hbm_budget_bytes=8 * 2 ** 30)
+    done = srv.run(_requests(3, 12, T))
+    assert len(done) == 12
+    assert srv.relayouts > srv.engine_builds and srv.engine_builds <= 6
+    br = srv.breakdown(1.0)
+    assert br["relayouts"] == srv.relayouts
+
+
 def test_admission_respects_budget(cuda):
     from dexdeform_gb300.serving import Server
     T = 10
