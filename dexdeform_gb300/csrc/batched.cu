@@ -91,6 +91,19 @@ __device__ __forceinline__ m33 ldm33(const float *__restrict__ S, int N, int pla
   for (int i = 0; i < 9; ++i) m.a[i / 3][i % 3] = __ldg(S + (size_t)(plane + i) * N + p);
   return m;
 }
+// A load that is not merged with an earlier one of the same address: the
+// caller reads the value again instead of keeping it in a register between.
+__device__ __forceinline__ float ld_again(const float *a) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(a));
+  return v;
+}
+__device__ __forceinline__ m33 ldm33_again(const float *S, int N, int plane, int p) {
+  m33 m;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m.a[i / 3][i % 3] = ld_again(S + (size_t)(plane + i) * N + p);
+  return m;
+}
 __device__ __forceinline__ void stm33(float *S, int N, int plane, int p, const m33 &m) {
 #pragma unroll
   for (int i = 0; i < 9; ++i) S[(size_t)(plane + i) * N + p] = m.a[i / 3][i % 3];
@@ -266,6 +279,31 @@ constexpr size_t kScatterSmemPerWarp = sizeof(float) * kRedWarpFloats;
 __device__ __forceinline__ float *warp_red_buffer() {
   extern __shared__ float4 s_dyn[];
   return reinterpret_cast<float *>(s_dyn) + (threadIdx.x >> 5) * kRedWarpFloats;
+}
+
+// Per-lane values parked in a column of shared memory (entry k at base[32 k]:
+// the 32 lanes of a warp hit 32 banks).
+__device__ __forceinline__ void stash3(float *base, int k, f3 a) {
+  base[32 * k] = a.x;
+  base[32 * (k + 1)] = a.y;
+  base[32 * (k + 2)] = a.z;
+}
+__device__ __forceinline__ f3 unstash3(const float *base, int k) {
+  return mk3(base[32 * k], base[32 * (k + 1)], base[32 * (k + 2)]);
+}
+__device__ __forceinline__ void stash33(float *base, int k, const m33 &a) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) base[32 * (k + 3 * r + c)] = a.a[r][c];
+}
+__device__ __forceinline__ m33 unstash33(const float *base, int k) {
+  m33 a;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a.a[r][c] = base[32 * (k + 3 * r + c)];
+  return a;
 }
 
 // This lane's position in the warp's segment order and the segment
@@ -954,11 +992,18 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_GRAD_MINB) k_grid_op_grad(Dex
 // gradient of state s + 1.  With kTape the SVD and stress of F_tmp come from
 // the tape the recomputed forward wrote (same values, without the SVD's
 // registers and arithmetic).  v: the particle's velocity in state s.
-template <bool kTape>
+//
+// With kStash (the fused kernel), the results the stress adjoint does not
+// touch -- the x and v gradients, the direct C gradient m Gs and v -- wait
+// across it in `stash` (this lane's column of the warp's shared scatter rows,
+// unused until the G2P adjoint: entry k at stash[32 k]) instead of in
+// registers; o_gx, o_gv and v are then not written (read them back with
+// unstash3 at 0, 3 and 15).
+template <bool kTape, bool kStash = false>
 __device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEnv &E, int p, const Stencil &st,
                                                   const float *__restrict__ S, const float *__restrict__ Gnext,
                                                   const float *G, const float *__restrict__ tape, f3 &v, f3 &o_gx,
-                                                  f3 &o_gv, m33 &o_gF, m33 &o_gC) {
+                                                  f3 &o_gv, m33 &o_gF, m33 &o_gC, float *stash = nullptr) {
   const int N = B.n_particles;
   v = ldf3(S, N, PV, p);
   const m33 C = ldm33(S, N, PC, p);
@@ -1069,19 +1114,35 @@ __device__ __forceinline__ void p2g_grad_particle(const DexBatch &B, const DexEn
     Gs.a[0][1] = c1.x; Gs.a[1][1] = c1.y; Gs.a[2][1] = c1.z;
     Gs.a[0][2] = c2.x; Gs.a[1][2] = c2.y; Gs.a[2][2] = c2.z;
   }
-  const m33 g_stress = Gs * gss, g_C = Gs * m;
+  const m33 g_stress = Gs * gss;
+  m33 g_C = Gs * m;
   const f3 g_v = gw * m;
+  if constexpr (kStash) {
+    stash3(stash, 0, ldf3(G, N, PX, p) + g_x);
+    stash3(stash, 3, g_v);
+    stash33(stash, 6, g_C);
+    stash3(stash, 15, v);
+  }
   if constexpr (kTape) forward_state();
 
   // stress and projection -> F_tmp gradient (integrator.cu:541-625)
-  const m33 Gt = plastic_stress_backward(sv, pl, g_stress, ldm33(Gnext, N, PF, p), mu, lam, ys);
+  const m33 Gt = kStash ? plastic_stress_backward_at(sv, pl, g_stress, [&]() { return ldm33_again(Gnext, N, PF, p); },
+                                                    mu, lam, ys)
+                        : plastic_stress_backward(sv, pl, g_stress, ldm33(Gnext, N, PF, p), mu, lam, ys);
   // F_tmp = (I + dt C) F
+  if constexpr (kStash) {
+    // F and C read again rather than held across the stress adjoint
+    g_C = unstash33(stash, 6);
+    F = ldm33_again(S, N, PF, p);
+  }
   const m33 gC_total = g_C + mm(Gt, mT(F)) * E.dt;
-  m33 IdtC = C * E.dt;
+  m33 IdtC = (kStash ? ldm33_again(S, N, PC, p) : C) * E.dt;
   IdtC.a[0][0] += 1.f; IdtC.a[1][1] += 1.f; IdtC.a[2][2] += 1.f;
   const m33 gF = mm(mT(IdtC), Gt);
-  o_gx = ldf3(G, N, PX, p) + g_x;
-  o_gv = g_v;
+  if constexpr (!kStash) {
+    o_gx = ldf3(G, N, PX, p) + g_x;
+    o_gv = g_v;
+  }
   o_gF = gF;
   o_gC = gC_total;
 }
@@ -1167,14 +1228,23 @@ __global__ void __launch_bounds__(128, DEX_P2G2G_GRAD_MINB) k_p2g2g_grad(DexBatc
   const bool in = loc < E.n;
   const int p = E.p_off + (in ? loc : 0);
   const f3 x = ldf3(S, N, PX, p);
-  const f3 xprev = ldf3(Sprev, N, PX, p);  // for the G2P adjoint, loaded ahead
+  // the G2P adjoint's position, loaded ahead and parked in shared memory
+  // with the P2G adjoint's results (this lane's column of the warp's scatter
+  // rows, entries 0-17 by p2g_grad_particle, 18-20 here)
+  float *stash = warp_red_buffer() + lane;
+  stash3(stash, 18, ldf3(Sprev, N, PX, p));
   Stencil st;
   make_stencil(x, E.inv_dx, st);
   const bool ok = in && stencil_in_grid(E, st);  // out-of-grid particles were reported by the G2P adjoint
   if (!ok) st.base[0] = st.base[1] = st.base[2] = 0;
   f3 v, gx, gv;
   m33 gF, gC;
-  p2g_grad_particle<kTape>(B, E, p, st, S, Gnext, G, tape, v, gx, gv, gF, gC);
+  p2g_grad_particle<kTape, true>(B, E, p, st, S, Gnext, G, tape, v, gx, gv, gF, gC, stash);
+  gx = unstash3(stash, 0);
+  gv = unstash3(stash, 3);
+  v = unstash3(stash, 15);
+  const f3 xprev = unstash3(stash, 18);
+  __syncwarp();  // every lane has its values back before the scatter rows are written
   if (ok) {
     stm33(G, N, PF, p, gF);
   } else {

@@ -336,6 +336,15 @@ DX_HD void jacobi_rotate(float S[3][3], m33 &V, int p, int q, int r) {
   }
 }
 
+// Whether every pivot of S is below jacobi_rotate's skip threshold: then a
+// sweep leaves S and V as they are, and so do all later sweeps.
+DX_HD bool jacobi_settled(const float S[3][3]) {
+  auto below = [&](int p, int q) {
+    return !(fabsf(S[p][q]) > fmaxf(5.9604645e-8f * fmaxf(fabsf(S[p][p]), fabsf(S[q][q])), 1e-30f));
+  };
+  return below(0, 1) && below(0, 2) && below(1, 2);
+}
+
 DX_HD void swap_neg_cols(m33 &M, int i, int j) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -384,8 +393,12 @@ DX_HD SVD3 svd3_from_deviation(const m33 &E) {
 #ifndef DEX_JACOBI_SWEEPS
 #define DEX_JACOBI_SWEEPS 4
 #endif
+  // a lane leaves the sweeps once they would no longer change anything (the
+  // result is that of all DEX_JACOBI_SWEEPS); a warp runs them while any of
+  // its lanes needs them
 #pragma unroll 1
   for (int sweep = 0; sweep < DEX_JACOBI_SWEEPS; ++sweep) {
+    if (jacobi_settled(S)) break;
     jacobi_rotate(S, o.V, 0, 1, 2);
     jacobi_rotate(S, o.V, 0, 2, 1);
     jacobi_rotate(S, o.V, 1, 2, 0);
@@ -772,8 +785,11 @@ DX_HD m33 svd_backward_rot(const SVD3 &sv, const float ku[3], const float kv[3],
 // V^T dL/dV: W - W^T and W^T - W, plus T E - (T E)^T and T^T E - (T^T E)^T
 // after a yield (T = U^T dL/dnewF V, E = diag(D)).  Not yielded, newF is F_tmp
 // itself and dL/dnewF passes to dL/dF_tmp directly.
-DX_HD m33 plastic_stress_backward(const SVD3 &sv, const Plastic &pl, const m33 &g_stress, const m33 &GF, float mu,
-                                  float lam, float ys) {
+// load_gf() returns dL/dnewF; it is called where the value is first needed
+// (so that a caller that reads it from memory need not hold it before).
+template <class LoadGF>
+DX_HD m33 plastic_stress_backward_at(const SVD3 &sv, const Plastic &pl, const m33 &g_stress, LoadGF load_gf,
+                                     float mu, float lam, float ys) {
   const m33 X = mm(mT(sv.U), mm(g_stress, sv.U));
   const f3 D3 = pl.expe, Dm3 = pl.dm1;
   const float Dv[3] = {D3.x, D3.y, D3.z}, Dm[3] = {Dm3.x, Dm3.y, Dm3.z};
@@ -793,7 +809,7 @@ DX_HD m33 plastic_stress_backward(const SVD3 &sv, const Plastic &pl, const m33 &
   }
   f3 g_s;
   if (pl.yielded) {
-    const m33 T = mm(mT(sv.U), mm(GF, sv.V)) + Q;
+    const m33 T = mm(mT(sv.U), mm(load_gf(), sv.V)) + Q;
     const f3 ee = pl.expe;
     const float ev[3] = {ee.x, ee.y, ee.z};
 #pragma unroll
@@ -820,8 +836,14 @@ DX_HD m33 plastic_stress_backward(const SVD3 &sv, const Plastic &pl, const m33 &
   } else {
     // dL/dF_tmp receives dL/dnewF directly: GF + U Q V^T
     g_s = mk3(g_J * sv.s.y * sv.s.z, g_J * sv.s.x * sv.s.z, g_J * sv.s.x * sv.s.y);
-    return GF + svd_backward_rot(sv, ku, kv, g_s, Q, true);
+    const m33 r = svd_backward_rot(sv, ku, kv, g_s, Q, true);
+    return load_gf() + r;
   }
+}
+
+DX_HD m33 plastic_stress_backward(const SVD3 &sv, const Plastic &pl, const m33 &g_stress, const m33 &GF, float mu,
+                                  float lam, float ys) {
+  return plastic_stress_backward_at(sv, pl, g_stress, [&]() { return GF; }, mu, lam, ys);
 }
 
 }  // namespace dexmpm

@@ -21,10 +21,10 @@
 //             scans) -- env e's blocks follow env e-1's, so block bases are
 //             global particle indices;
 //   place  -- perm[base(block) + start(cell) + rank] = old index;
-//   fix    -- per occupied block (a warp): each cell's segment of perm put in
-//             increasing old index (the ranks came from atomics in arbitrary
-//             order); then the counts, totals, flags and list are zeroed for
-//             the next sort;
+//   fix    -- per occupied block (a warp; a CTA for large blocks): each
+//             cell's segment of perm put in increasing old index (the ranks
+//             came from atomics in arbitrary order); then the counts, totals,
+//             flags and list are zeroed for the next sort;
 //   permute -- the 24 state planes gathered into the new order.
 // The caller permutes whatever else is per particle (material, targets) with
 // dexmpm_permute and the same perm.
@@ -184,20 +184,26 @@ __global__ void __launch_bounds__(256) k_sort_place(DexBatch B, DexSortWork W, i
   perm[W.block_base[ci >> 6] + W.cell_start[ci] + W.rank[p]] = p;
 }
 
-// Per occupied block (one warp): each of its cells' segments of perm put in
-// increasing old index, then the cell counts, block total and flag cleared.
-// The ranks within a cell came from atomics in arbitrary order.  The block's
-// entries (contiguous in perm, cell after cell) are staged in the warp's
-// shared-memory row in one coalesced pass; each lane checks whether its two
-// cells are already in order (the usual case after an env step of drift)
-// and the warp then places the entries of each out-of-order cell at their
-// rank -- the number of smaller entries (old indices are distinct) -- each
-// lane counting for every 32nd entry.  A block of more than kFixRow entries
-// is done cell by cell with the same steps; a cell of more than kFixRow is
-// insertion-sorted in place by one lane.  The last CTA to finish resets the
-// list count and its own ticket.
+// Per occupied block: each of its cells' segments of perm put in increasing
+// old index, then the cell counts, block total and flag cleared.  The ranks
+// within a cell came from atomics in arbitrary order.  The block's entries
+// (contiguous in perm, cell after cell) are staged in shared memory in one
+// coalesced pass; a cell whose staged entries are already in order (the
+// usual case after an env step of drift) is left alone, the entries of any
+// other cell are placed at their rank -- the number of smaller entries (old
+// indices are distinct) -- each lane counting for every 32nd entry.
+//   k_sort_fix      one warp per block of at most kFixRow entries, staged in
+//                   the warp's row of shared memory; larger blocks are left;
+//   k_sort_fix_big  one CTA per block of more than kFixRow entries, staged in
+//                   the CTA's whole shared memory (kFixWarps * kFixRow
+//                   entries), its warps taking every kFixWarps-th cell; a
+//                   block larger still is done cell by cell (a cell of more
+//                   than kFixRow entries insertion-sorted in place by one
+//                   lane).  The last CTA to finish resets the list count and
+//                   its own ticket.
 constexpr int kFixRow = 1024;
 constexpr int kFixWarps = 8;  // 256-thread CTAs
+constexpr int kFixAll = kFixRow * kFixWarps;
 
 // Ranks of the n entries row[0 .. n) written to seg[rank] (warp-wide).
 __device__ __forceinline__ void place_by_rank(const int32_t *row, int32_t *seg, int n, int lane) {
@@ -209,6 +215,24 @@ __device__ __forceinline__ void place_by_rank(const int32_t *row, int32_t *seg, 
   }
 }
 
+// The cell (n entries staged at row[0 .. n), perm segment seg) put in order
+// by the calling warp, unless its entries already are.
+__device__ __forceinline__ void fix_cell(const int32_t *row, int32_t *seg, int n, int lane) {
+  bool ordered = true;
+  for (int i = lane; i + 1 < n; i += 32) ordered = ordered && row[i] < row[i + 1];
+  if (!__all_sync(kFull, ordered)) place_by_rank(row, seg, n, lane);
+}
+
+// Cell counts, block total and flag of a finished block back to zero.
+__device__ __forceinline__ void clear_block(DexSortWork &W, int blk, int lane) {
+  W.cell_count[(blk << 6) + lane] = 0;
+  W.cell_count[(blk << 6) + 32 + lane] = 0;
+  if (lane == 0) {
+    W.block_total[blk] = 0;
+    W.block_flag[blk] = 0u;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__restrict__ perm) {
   __shared__ int32_t rows[kFixWarps][kFixRow];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -217,36 +241,79 @@ __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__rest
   const int cnt = *reinterpret_cast<volatile int32_t *>(W.counters);
   for (int item = blockIdx.x * kFixWarps + wid; item < cnt; item += warps) {
     const int blk = W.block_list[item];
-    const int base = W.block_base[blk];
     const int total = W.block_total[blk];
+    if (total > kFixRow) continue;  // k_sort_fix_big
+    const int base = W.block_base[blk];
     // lane l owns cells l and l + 32 of the block
     const int n0 = W.cell_count[(blk << 6) + lane], n1 = W.cell_count[(blk << 6) + 32 + lane];
     const int st0 = W.cell_start[(blk << 6) + lane], st1 = W.cell_start[(blk << 6) + 32 + lane];
-    if (total <= kFixRow) {
-      for (int i = lane; i < total; i += 32) row[i] = perm[base + i];
-      __syncwarp();
-      bool ok0 = true, ok1 = true;
-      for (int a = 1; a < n0; ++a) ok0 = ok0 && row[st0 + a - 1] < row[st0 + a];
-      for (int a = 1; a < n1; ++a) ok1 = ok1 && row[st1 + a - 1] < row[st1 + a];
-      const unsigned bad[2] = {__ballot_sync(kFull, !ok0), __ballot_sync(kFull, !ok1)};
+#pragma unroll 4
+    for (int i = lane; i < total; i += 32) row[i] = perm[base + i];
+    __syncwarp();
+    bool ok0 = true, ok1 = true;
+    for (int a = 1; a < n0; ++a) ok0 = ok0 && row[st0 + a - 1] < row[st0 + a];
+    for (int a = 1; a < n1; ++a) ok1 = ok1 && row[st1 + a - 1] < row[st1 + a];
+    const unsigned bad[2] = {__ballot_sync(kFull, !ok0), __ballot_sync(kFull, !ok1)};
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        for (unsigned rest = bad[h]; rest; rest &= rest - 1u) {
-          const int owner = __ffs(rest) - 1;
-          const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
-          const int st = __shfl_sync(kFull, h ? st1 : st0, owner);
-          place_by_rank(row + st, perm + base + st, n, lane);
-        }
+    for (int h = 0; h < 2; ++h) {
+      for (unsigned rest = bad[h]; rest; rest &= rest - 1u) {
+        const int owner = __ffs(rest) - 1;
+        const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
+        const int st = __shfl_sync(kFull, h ? st1 : st0, owner);
+        place_by_rank(row + st, perm + base + st, n, lane);
       }
-      __syncwarp();
-    } else {
-      const unsigned todo[2] = {__ballot_sync(kFull, n0 > 1), __ballot_sync(kFull, n1 > 1)};
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        for (unsigned rest = todo[h]; rest; rest &= rest - 1u) {
-          const int owner = __ffs(rest) - 1;
-          const int n = __shfl_sync(kFull, h ? n1 : n0, owner);
-          int32_t *seg = perm + base + __shfl_sync(kFull, h ? st1 : st0, owner);
+    }
+    __syncwarp();
+    clear_block(W, blk, lane);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sort_fix_big(DexSortWork W, int32_t *__restrict__ perm) {
+  __shared__ int32_t all[kFixAll];
+  __shared__ int32_t big[256];               // this window's large blocks
+  __shared__ int32_t cnt_c[64], start_c[64];  // the block's cell counts and starts
+  __shared__ int n_big;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int cnt = *reinterpret_cast<volatile int32_t *>(W.counters);
+  // windows of blockDim.x list entries, one per thread, the CTAs taking
+  // every gridDim.x-th entry (so that the large blocks spread over all of
+  // them): the window's large blocks (k_sort_fix cleared the others' totals)
+  // are collected, then done one after the other by the whole CTA
+  const int stride = gridDim.x * blockDim.x;
+  for (int first = blockIdx.x; first < cnt; first += stride) {
+    if (threadIdx.x == 0) n_big = 0;
+    __syncthreads();
+    const int item = first + gridDim.x * threadIdx.x;
+    if (item < cnt) {
+      const int blk = W.block_list[item];
+      if (W.block_total[blk] > kFixRow) big[atomicAdd(&n_big, 1)] = blk;
+    }
+    __syncthreads();
+    const int nb = n_big;
+    for (int k = 0; k < nb; ++k) {
+      const int blk = big[k];
+      const int total = W.block_total[blk];  // the same for every thread of the CTA
+      const int base = W.block_base[blk];
+      if (threadIdx.x < 64) {
+        cnt_c[threadIdx.x] = W.cell_count[(blk << 6) + threadIdx.x];
+        start_c[threadIdx.x] = W.cell_start[(blk << 6) + threadIdx.x];
+      }
+      if (total <= kFixAll) {
+#pragma unroll 4
+        for (int i = threadIdx.x; i < total; i += blockDim.x) all[i] = perm[base + i];
+      }
+      __syncthreads();
+      if (total <= kFixAll) {
+        for (int c = wid; c < 64; c += kFixWarps) {
+          const int n = cnt_c[c];
+          if (n > 1) fix_cell(all + start_c[c], perm + base + start_c[c], n, lane);
+        }
+      } else {
+        int32_t *row = all + wid * kFixRow;
+        for (int c = wid; c < 64; c += kFixWarps) {
+          const int n = cnt_c[c];
+          if (n < 2) continue;
+          int32_t *seg = perm + base + start_c[c];
           if (n > kFixRow) {
             if (lane == 0) {
               for (int a = 1; a < n; ++a) {
@@ -264,18 +331,12 @@ __global__ void __launch_bounds__(256) k_sort_fix(DexSortWork W, int32_t *__rest
           }
           for (int i = lane; i < n; i += 32) row[i] = seg[i];
           __syncwarp();
-          bool ordered = true;
-          for (int i = lane; i + 1 < n; i += 32) ordered = ordered && row[i] < row[i + 1];
-          if (!__all_sync(kFull, ordered)) place_by_rank(row, seg, n, lane);
+          fix_cell(row, seg, n, lane);
           __syncwarp();
         }
       }
-    }
-    W.cell_count[(blk << 6) + lane] = 0;
-    W.cell_count[(blk << 6) + 32 + lane] = 0;
-    if (lane == 0) {
-      W.block_total[blk] = 0;
-      W.block_flag[blk] = 0u;
+      __syncthreads();  // the block's cells are done before the staging is reused
+      if (wid == 0) clear_block(W, blk, lane);
     }
   }
   __syncthreads();
@@ -354,6 +415,8 @@ int dexmpm_sort(const DexBatch *b, const DexSortWork *w, const float *s, float *
     if (int rc = check_launch()) return rc;
   }
   k_sort_fix<<<persistent, 256, 0, st>>>(*w, perm);
+  if (int rc = check_launch()) return rc;
+  k_sort_fix_big<<<persistent, 256, 0, st>>>(*w, perm);
   if (int rc = check_launch()) return rc;
   return dexmpm_permute(perm, s, sorted_s, b->n_particles, DEXMPM_STATE_PLANES, 0, stream);
 }

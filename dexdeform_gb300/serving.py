@@ -151,7 +151,7 @@ class Server:
     """Continuous-batching MPM server on one GPU."""
 
     def __init__(self, substeps=50, hbm_budget_bytes=180 * 2 ** 30, device="cuda", tile_size=128,
-                 use_graphs=True, max_inflight_rounds=3, capture_after=3, growth=1.25):
+                 use_graphs=True, max_inflight_rounds=3, capture_after=8, growth=1.25):
         self.T = substeps
         self.budget = int(hbm_budget_bytes)
         self.device = torch.device(device)
@@ -216,7 +216,11 @@ class Server:
         need = Capacity.of([r.spec for r in reqs], self.tile_size)
         if a is None or not a.E.capacity.holds(need):
             t0 = time.perf_counter()
-            cap = need.scaled(self.growth)
+            # room for every admitted request that can join this phase (all
+            # of them forward, the gradient requests backward), so that the
+            # arena is not regrown at each admission
+            can_join = [r.spec for r in self.running.values() if r.grad or not grad]
+            cap = need.union(Capacity.of(can_join, self.tile_size)).scaled(self.growth)
             if a is not None:
                 cap = cap.union(a.E.capacity)
             a = _Arena(cap, self.T, grad, self.device, self.tile_size, self.use_graphs, self.capture_after)

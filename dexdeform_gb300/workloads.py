@@ -239,14 +239,37 @@ def tiny_env(seed=0, n=256, grid=32, nb=4, steps=4, dt=1e-4, shape="cube"):
                     extent=(0.12, 0.06, 0.09), nb=nb, steps=steps, name=f"tiny{grid}e")
 
 
-def perturb_state(env: Env, seed=1, v_scale=0.5, c_scale=5.0, f_scale=0.05):
-    """A non-rest state (random v, C and F near identity) for adjoint checks,
-    where F = I would put the SVD at its degenerate point."""
+def random_rotations(rng, n):
+    """n uniformly random proper rotations (normalised Gaussian quaternions)."""
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+                     np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+                     np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def perturb_state(env: Env, seed=1, v_scale=0.5, c_scale=5.0, f_scale=0.05, f_mode="separated"):
+    """A non-rest state for adjoint checks: random v and C, and F away from
+    the identity (F = I puts the SVD at its degenerate point).
+    f_mode "separated": F = U diag(s) V^T with random rotations U, V and
+    singular values s = 1 + f_scale (k + u), k = 1, 0, -1, u ~ U[-1/4, 1/4],
+    so that every gap is at least f_scale / 2 (nearly equal singular values
+    make the SVD adjoint -- the reference's and this one -- divide FP32
+    rounding by their squared difference).  "gaussian": F = I + f_scale N(0,
+    1) entrywise (the states of the committed oracle fixtures)."""
     rng = np.random.default_rng(seed)
     st = env.state()
+    n = st["F"].shape[0]
     st["v"] = (rng.normal(size=st["v"].shape) * v_scale).astype(np.float32)
     st["C"] = (rng.normal(size=st["C"].shape) * c_scale).astype(np.float32)
-    st["F"] = (np.eye(3) + rng.normal(size=st["F"].shape) * f_scale).astype(np.float32)
+    if f_mode == "gaussian":
+        st["F"] = (np.eye(3) + rng.normal(size=st["F"].shape) * f_scale).astype(np.float32)
+        return st
+    assert f_mode == "separated"
+    s = 1.0 + f_scale * (np.array([1.0, 0.0, -1.0]) + rng.uniform(-0.25, 0.25, (n, 3)))
+    U, V = random_rotations(rng, n), random_rotations(rng, n)
+    st["F"] = np.einsum("nij,nj,nkj->nik", U, s, V).astype(np.float32)
     return st
 
 

@@ -53,7 +53,7 @@ def rollout_fixture(name, env, steps, keep=(1,)):
 
 def grad_fixture(name, env, seed=7):
     r = sim(env)
-    st = W.perturb_state(env, seed=seed, v_scale=0.1, c_scale=1.0, f_scale=0.02)
+    st = W.perturb_state(env, seed=seed, v_scale=0.1, c_scale=1.0, f_scale=0.02, f_mode="gaussian")
     nxt = r.substep(st, env.pose(0), env.pose(1))
     rng = np.random.default_rng(seed + 1)
     g_next = {k: rng.normal(size=st[k].shape).astype(np.float32) for k in st}

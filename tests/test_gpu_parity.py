@@ -469,25 +469,29 @@ def test_fused_substeps_equal_unfused(cuda):
 def test_fused_adjoint_equals_unfused(cuda, T):
     """BatchEngine.run_adjoint (each P2G adjoint fused with the previous
     substep's G2P adjoint, the x, v, C gradients passed in registers) against
-    the same T adjoint substeps launched one kernel at a time, after the same
-    kept forward with a tape (T = 1: no fused launch; T = 2: one)."""
+    the same T adjoint substeps launched one kernel at a time (T = 1: no fused
+    launch; T = 2: one).  Both run on the same kept forward: its grid slots,
+    lists, states and tape are saved after it and put back before the second
+    adjoint, so that only the adjoints differ."""
     from dexdeform_gb300 import workloads as W
     from dexdeform_gb300.engine import BatchEngine, EnvSpec
     envs = W.batch_envs(7, n_envs=3, steps=10, n_lo=500, n_hi=3000)
+    E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=T + 2)
+    poses = torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
+                         device="cuda")
+    sts = E.new_slots(T + 1)
+    sts[0].copy_(E.pack_state([W.perturb_state(e, seed=3, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs]))
+    tapes = E.new_tape(T)
+    E.run_substeps([sts[t] for t in range(T + 1)], poses, kept=True, tapes=tapes)
+    kept = [t.clone() for t in (E.grid, E.vout, E.block_flag, E.block_list, E.block_count)]
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    g_final = torch.randn(sts[T].shape, device="cuda", generator=gen)
+    nb = max(E.n_bodies, 1)
     outs = []
     for mode in ("unfused", "fused"):
-        E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=T + 2)
-        poses = torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
-                             device="cuda")
-        sts = E.new_slots(T + 1)
-        sts[0].copy_(E.pack_state([W.perturb_state(e, seed=3, v_scale=0.1, c_scale=1.0, f_scale=0.02)
-                                   for e in envs]))
-        tapes = E.new_tape(T)
-        E.run_substeps([sts[t] for t in range(T + 1)], poses, kept=True, tapes=tapes)
-        gen = torch.Generator(device="cuda").manual_seed(11)
-        g_next = torch.randn(sts[T].shape, device="cuda", generator=gen)
-        g = torch.zeros_like(g_next)
-        nb = max(E.n_bodies, 1)
+        for dst, src in zip((E.grid, E.vout, E.block_flag, E.block_list, E.block_count), kept):
+            dst.copy_(src)
+        g_next, g = g_final.clone(), torch.zeros_like(g_final)
         bg = torch.zeros((T + 1, nb, 8), device="cuda")
         if mode == "unfused":
             for s in range(T - 1, -1, -1):
@@ -500,10 +504,10 @@ def test_fused_adjoint_equals_unfused(cuda, T):
         assert E.error_word() == 0
         assert int(E.block_count[2:].sum()) == 0  # the adjoint cleared every kept slot
         n = sum(sp.n for sp in E.specs)  # the state layout pads the particle count to a multiple of 32
-        outs.append((sts[T][:, :n].clone(), out[:, :n].clone(), bg.clone()))
-    # float-atomic ordering only (see the kept-env-step test for the levels)
-    (sa, ga, ba), (sb, gb, bb) = outs
-    assert rel(sa.cpu().numpy(), sb.cpu().numpy()) < 2e-4
+        outs.append((out[:, :n].clone(), bg.clone()))
+    # the same arithmetic; the float atomics of the adjoint grids add in
+    # another order in each run
+    (ga, ba), (gb, bb) = outs
     assert rel(ga.cpu().numpy(), gb.cpu().numpy()) < 5e-4
     assert rel(ba.cpu().numpy(), bb.cpu().numpy()) < 5e-4
 

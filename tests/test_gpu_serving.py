@@ -111,7 +111,7 @@ def test_serving_relays_out_instead_of_rebuilding(cuda):
     srv = Server(substeps=T, hbm_budget_bytes=8 * 2 ** 30)
     done = srv.run(_requests(3, 12, T))
     assert len(done) == 12
-    assert srv.relayouts > srv.engine_builds and srv.engine_builds <= 6
+    assert srv.relayouts > 2 * srv.engine_builds
     br = srv.breakdown(1.0)
     assert br["relayouts"] == srv.relayouts
 

@@ -46,6 +46,25 @@ def expected_perm(E, state):
     return perm
 
 
+def block_and_cell_sizes(E, state):
+    """Largest 4^3-block population, every block's population, largest cell
+    population of the sort keys."""
+    x = state[0:3].cpu().numpy().astype(np.float32)
+    blocks, cells = [], []
+    for e, s in enumerate(E.specs):
+        o, n = E.p_off[e], s.n
+        f = np.floor((x[:, o:o + n] * np.float32(1.0 / s.dx)).astype(np.float32) - np.float32(0.5))
+        g = np.asarray(s.grid_dim)[:, None]
+        c = np.where(f >= 0, np.minimum(f, g - 1), 0).astype(np.int64)
+        blk = ((c[0] >> 2) * (s.grid_dim[1] // 4) + (c[1] >> 2)) * (s.grid_dim[2] // 4) + (c[2] >> 2)
+        cell = (c[0] * s.grid_dim[1] + c[1]) * s.grid_dim[2] + c[2]
+        bc = np.bincount(blk)
+        blocks.append(bc[bc > 0])
+        cells.append(np.bincount(cell).max())
+    b = np.concatenate(blocks)
+    return int(b.max()), b, int(max(cells))
+
+
 def _engine(envs, **kw):
     from dexdeform_gb300.engine import BatchEngine, EnvSpec
     return BatchEngine([EnvSpec.from_env(e) for e in envs], **kw)
@@ -56,10 +75,21 @@ def test_sort_matches_numpy_order_and_permutes_exactly(cuda):
     envs = W.batch_envs(11, n_envs=5, steps=1, n_lo=300, n_hi=5000, sort=False)
     envs.append(W.make_env(3, 1500, "cube", grid=32, center=(0.5, 0.2, 0.5), extent=0.3, nb=3, steps=1,
                            sort=False))
+    # dense clusters: 4^3 blocks of 1,024 - 8,192 particles (staged by a whole
+    # CTA), of more than 8,192 (cell by cell), and cells of more than 1,024
+    # (insertion sort in place)
+    envs.append(W.make_env(4, 6000, "cube", grid=32, center=(0.5, 0.3, 0.5), extent=0.12, nb=1, steps=1,
+                           sort=False))
+    envs.append(W.make_env(5, 12000, "cube", grid=32, center=(0.41, 0.41, 0.41), extent=0.06, nb=1, steps=1,
+                           sort=False))
+    envs.append(W.make_env(6, 20000, "cube", grid=32, center=(0.453, 0.453, 0.453), extent=0.07, nb=1, steps=1,
+                           sort=False))
     envs[1].x = envs[1].x.copy()
     envs[1].x[7] = (2.0, -0.5, np.nan)   # outside the grid on every axis: clamped, still sorted
     E = _engine(envs)
     s = E.pack_state([e.state() for e in envs])
+    sizes = block_and_cell_sizes(E, s)
+    assert sizes[0] > 8192 and ((sizes[1] > 1024) & (sizes[1] <= 8192)).any() and sizes[2] > 1024, sizes[::2]
     out = torch.zeros_like(s)
     perm = E.identity_perm(1)[0]
     E.sort(s, out, perm)
