@@ -603,7 +603,8 @@ def serving_leg(dev, seed=0, n_req=200, rate_hz=20.0):
             "rate_hz": rate_hz, "wall_s": round(wall, 3), "rounds": srv.rounds,
             "breakdown": srv.breakdown(wall),
             "peak_hbm_gb": round((torch.cuda.max_memory_allocated(dev) - base) / 2 ** 30, 3),
-            "hbm_budget_gb": 180, "what": "Poisson arrivals, 48/64/96^3 grids, 2k-50k particles, horizons 5-100 env "
+            "hbm_budget_gb": 180, "what": "Poisson arrivals, 48/64/96^3 grids, 2k-50k particles in sampling order "
+                                          "(sorted by grid cell on the device each round), horizons 5-100 env "
                                           "steps x 50 substeps, 30% gradient requests; continuous batching"}
 
 

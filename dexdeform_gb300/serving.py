@@ -86,10 +86,15 @@ class _Resident:
 class _Arena:
     """One phase's BatchEngine (forward, or adjoint with kept grid slots) with
     its round buffers, sized to a capacity and re-laid out for each new
-    membership, plus the CUDA graphs of the current membership."""
+    membership, plus the CUDA graphs of the current membership.
+
+    With `sort`, a round orders the gathered particles by grid cell on the
+    device first (BatchEngine.sort; material and incoming gradients permuted
+    the same way), steps them in that order and maps the results back, so
+    that requests may hand over their particles in any order."""
 
     def __init__(self, capacity: Capacity, substeps: int, grad: bool, device, tile_size: int, use_graphs: bool,
-                 capture_after: int):
+                 capture_after: int, sort: bool = True):
         self.E = BatchEngine([], device=device, grad=grad, tile_size=tile_size,
                              grid_slots=substeps + 2 if grad else 2, capacity=capacity)
         self.T = substeps
@@ -102,6 +107,18 @@ class _Arena:
             self.gbuf = self.E.new_slots(2, zero=False)
             self.tape = self.E.new_tape(self.T, zero=False)
             self.bgrad = torch.zeros((self.T + 1, nb, 8), device=device)
+        self.sort = sort
+        E = self.E
+        if sort:
+            self.ident = E.identity_perm(1)[0]
+            self.perm = self.ident.clone()
+            self.srt = E.new_slots(1, zero=False)[0]      # state 0 in cell order
+            self.mat_s = torch.empty_like(E.mat)           # material in cell order
+            E.use_material(self.mat_s)
+            if grad:
+                self.gsrt = E.new_slots(1, zero=False)[0]  # incoming gradient in cell order
+        # where a round leaves its result in the requests' order
+        self.out = self.slot[0] if sort else self.slot[self.T]
         self.use_graphs = use_graphs
         self.capture_after = max(1, int(capture_after))
         self.key = None
@@ -119,20 +136,45 @@ class _Arena:
         for e, r in enumerate(reqs):
             o = E.p_off[e]
             E.mat[:, o:o + r.env.n].copy_(resident[r.rid].mat)
+        if self.sort:
+            # the sort writes the envs' entries; the rest stays the identity
+            self.perm.copy_(self.ident)
         self.key = key
         self.graphs.clear()
         self.uses.clear()
         return True
 
+    def _states(self):
+        """The round's states: sorted state 0, then the substeps' slots."""
+        first = self.srt if self.sort else self.slot[0]
+        return [first] + [self.slot[s] for s in range(1, self.T + 1)]
+
+    def _order(self):
+        E = self.E
+        E.sort(self.slot[0], self.srt, self.perm)
+        E.permute(self.perm, E.mat, self.mat_s)
+
     def _forward(self):
-        self.E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses)
+        E = self.E
+        if self.sort:
+            self._order()
+        E.run_substeps(self._states(), self.poses)
+        if self.sort:
+            E.permute(self.perm, self.slot[self.T], self.slot[0], inverse=True)
 
     def _backward(self):
         E = self.E
-        E.run_substeps([self.slot[s] for s in range(self.T + 1)], self.poses, kept=True, tapes=self.tape)
-        out = E.run_adjoint([self.slot[s] for s in range(self.T + 1)], self.gbuf[1], self.gbuf[0], self.poses,
-                            self.bgrad, tapes=self.tape)
-        if out is not self.gbuf[1]:
+        g_next = self.gbuf[1]
+        if self.sort:
+            self._order()
+            E.permute(self.perm, self.gbuf[1], self.gsrt)
+            g_next = self.gsrt
+        sts = self._states()
+        E.run_substeps(sts, self.poses, kept=True, tapes=self.tape)
+        out = E.run_adjoint(sts, g_next, self.gbuf[0], self.poses, self.bgrad, tapes=self.tape)
+        if self.sort:
+            E.permute(self.perm, out, self.gbuf[1], inverse=True)
+        elif out is not self.gbuf[1]:
             self.gbuf[1].copy_(out)
 
     def run(self, kind: str) -> bool:
@@ -151,7 +193,7 @@ class Server:
     """Continuous-batching MPM server on one GPU."""
 
     def __init__(self, substeps=50, hbm_budget_bytes=180 * 2 ** 30, device="cuda", tile_size=128,
-                 use_graphs=True, max_inflight_rounds=3, capture_after=8, growth=1.25):
+                 use_graphs=True, max_inflight_rounds=3, capture_after=8, growth=1.25, sort=True):
         self.T = substeps
         self.budget = int(hbm_budget_bytes)
         self.device = torch.device(device)
@@ -167,6 +209,7 @@ class Server:
         self.arenas: Dict[bool, _Arena] = {}
         self.capture_after = capture_after
         self.growth = float(growth)
+        self.sort = sort
         self.s_fwd = torch.cuda.Stream(device=self.device)
         self.s_bwd = torch.cuda.Stream(device=self.device)
         self.rounds = 0
@@ -223,7 +266,7 @@ class Server:
             cap = need.union(Capacity.of(can_join, self.tile_size)).scaled(self.growth)
             if a is not None:
                 cap = cap.union(a.E.capacity)
-            a = _Arena(cap, self.T, grad, self.device, self.tile_size, self.use_graphs, self.capture_after)
+            a = _Arena(cap, self.T, grad, self.device, self.tile_size, self.use_graphs, self.capture_after, self.sort)
             self.arenas[grad] = a
             self.engine_builds += 1
             self.host_build_s += time.perf_counter() - t0
@@ -263,7 +306,7 @@ class Server:
         for e, r in enumerate(reqs):
             res = self.resident[r.rid]
             o = E.p_off[e]
-            res.state.copy_(b.slot[self.T][:, o:o + r.env.n])
+            res.state.copy_(b.out[:, o:o + r.env.n])
             if r.grad:
                 res.ckpt.append(res.state.clone())
             self.work += r.env.n * self.T
@@ -427,10 +470,11 @@ def latency_stats(done: List[Request]):
 
 
 def poisson_requests(seed=0, n=32, rate_hz=20.0, grids=(48, 64, 96), n_lo=2000, n_hi=50000, h_lo=5, h_hi=100,
-                     grad_frac=0.3, substeps=50, horizon_scale=1.0):
+                     grad_frac=0.3, substeps=50, horizon_scale=1.0, sort=False):
     """Seeded serving workload: Poisson arrivals, grids 48/64/96^3, particles
     log-uniform in [n_lo, n_hi], horizons uniform in [h_lo, h_hi] env steps
-    (scaled by horizon_scale), grad_frac of the requests ask for gradients."""
+    (scaled by horizon_scale), grad_frac of the requests ask for gradients.
+    Particles in sampling order (sort=False) or presorted by grid cell."""
     from . import workloads as W
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -443,9 +487,9 @@ def poisson_requests(seed=0, n=32, rate_hz=20.0, grids=(48, 64, 96), n_lo=2000, 
         grad = bool(rng.random() < grad_frac)
         if rng.random() < 0.5:
             env = W.make_env(seed * 100000 + i, npart, "cube", grid=g, center=(0.5, 0.16, 0.5), extent=0.18,
-                             steps=h * substeps, name=f"req{i}")
+                             steps=h * substeps, sort=sort, name=f"req{i}")
         else:
             env = W.make_env(seed * 100000 + i, npart, "ellipsoid", grid=g, center=(0.5, 0.13, 0.5),
-                             extent=(0.12, 0.06, 0.09), steps=h * substeps, name=f"req{i}")
+                             extent=(0.12, 0.06, 0.09), steps=h * substeps, sort=sort, name=f"req{i}")
         out.append(Request(rid=i, env=env, horizon=h, grad=grad, arrival=t))
     return out
