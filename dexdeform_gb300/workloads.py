@@ -160,7 +160,7 @@ def make_env(seed, n, shape="cube", grid=64, dt=5e-5, yield_stress=50.0, center=
     if sort:
         x = x[cell_sort(x, dx)]
     mu, lam = lame(E, nu)
-    pv = volume / n
+    pv = volume / max(n, 1)
     tfsr, args = capsules(rng, nb)
     c = np.asarray(center)
     poses = random_walk_poses(rng, nb, steps, dt, lo=(c[0] - 0.12, top - 0.02, c[2] - 0.12),
