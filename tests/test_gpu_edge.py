@@ -39,6 +39,17 @@ def _envs():
     return [a, empty, bodyless, c]
 
 
+def _seeded_gradient(env):
+    """A gradient of the final state on every field, seeded by the env (so
+    that it is the same whatever batch the env is in).  A uniform one (1 on
+    every x and v) would leave the F and C gradients of a freely falling
+    body as FP32 residues of cancelling node sums (sum_n N_n dpos_n = 0)."""
+    rng = np.random.default_rng(1000 + int(env.n))
+    return {"x": rng.normal(size=(env.n, 3)).astype(np.float32), "v": rng.normal(size=(env.n, 3)).astype(np.float32),
+            "F": rng.normal(size=(env.n, 3, 3)).astype(np.float32),
+            "C": rng.normal(size=(env.n, 3, 3)).astype(np.float32)}
+
+
 def _run(envs):
     """Forward + backward of S env steps x T substeps; per env: final state,
     gradient of the initial state, body-pose gradients."""
@@ -49,8 +60,7 @@ def _run(envs):
     R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs], [e.poses[:, :, 3:] for e in envs]),
                                device="cuda")[:S * T + 1])
     s0 = E.pack_state([W.perturb_state(e, seed=9, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs])
-    g = torch.zeros_like(s0)
-    g[0:6] = 1.0
+    g = E.pack_state([_seeded_gradient(e) for e in envs])
     fin = E.unpack_state(R.forward(s0).clone())
     g0 = E.unpack_state(R.backward(g).clone())
     bg = R.bgrad.cpu().numpy()

@@ -280,10 +280,11 @@ def test_graph_replay_equals_eager(cuda):
         R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs],
                                                 [e.poses[:, :, 3:] for e in envs]), device="cuda"))
         s0 = E.pack_state([e.state() for e in envs])
+        # a per-particle x and v gradient, the same in both runs
+        g = torch.zeros_like(s0)
+        g[0:6] = torch.randn(g[0:6].shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
         for _ in range(3):  # eager+capture, then replays
             fin = R.forward(s0).clone()
-            g = torch.zeros_like(s0)
-            g[0:3] = 1.0
             g0 = R.backward(g).clone()
         outs.append((fin, g0, R.bgrad.clone()))
         assert E.error_word() == 0
@@ -412,8 +413,9 @@ def test_kept_last_env_step_equals_recompute(cuda):
         R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs],
                                                 [e.poses[:, :, 3:] for e in envs]), device="cuda"))
         s0 = E.pack_state([W.perturb_state(e, seed=3, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs])
+        # a per-particle x and v gradient, the same in every variant
         g = torch.zeros_like(s0)
-        g[0:6] = 1.0
+        g[0:6] = torch.randn(g[0:6].shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(4))
         for _ in range(2):
             for op in pattern:
                 if op == "f":

@@ -59,8 +59,7 @@ def _run(E, envs, T, grad):
         return (sts[T].clone(),)
     tape = E.new_tape(T)
     E.run_substeps(list(sts), poses, kept=True, tapes=tape)
-    g = torch.zeros_like(s0)
-    g[0:6] = 1.0
+    g = torch.randn(s0.shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(6))
     scratch = torch.zeros_like(s0)
     bgrad = torch.zeros_like(poses)
     out = E.run_adjoint(list(sts), g, scratch, poses, bgrad, tapes=tape)

@@ -151,8 +151,9 @@ def _rollout_pair(envs, T, S, state0_fn, grad=True):
         R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs],
                                                 [e.poses[:, :, 3:] for e in envs]), device="cuda")[:S * T + 1])
         s0 = E.pack_state(state0_fn())
-        g = torch.zeros_like(s0)
-        g[0:6] = 1.0
+        # a per-particle gradient on every field, the same in every variant
+        # (a uniform one would hide particles handed back in another order)
+        g = torch.randn(s0.shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
         for _ in range(2):  # eager + capture, then a replay
             fin = R.forward(s0).clone()
             g0 = R.backward(g).clone() if grad else None
