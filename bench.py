@@ -511,6 +511,21 @@ NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 
 NCU_L2_RED = {"g2p2g": (3212980, 5181759, 10.93), "g2p2g_tape": (3215606, 5185041, 10.06),
               "p2g2g_grad": (3208150, 5169492, 7.56)}
 
+# what limits each dominant kernel function, from its ncu capture on the same
+# batch (--set full): issue-active and DRAM throughput percentages, warps
+# active, and the reading of the stall counters
+NCU_LIMITER = {
+    "k_g2p2g": {"issue_active_pct": {"tape": 57.4, "forward": 60.9}, "dram_throughput_pct": {"tape": 19.8, "forward": 9.4},
+                "warps_active_pct": 33.3,
+                "reading": "instruction issue: G2P gather, SVD, return mapping and the 27-node scatter; "
+                           "long-scoreboard the top stall",
+                "source": "profiles/k_g2p2g_batch64.md"},
+    "k_p2g2g_grad": {"issue_active_pct": 49.8, "dram_throughput_pct": 24.9, "warps_active_pct": 28.4,
+                     "reading": "latency: streamed planes and dependent stress/SVD adjoint arithmetic at 20 "
+                                "warps per SM",
+                     "source": "profiles/k_p2g2g_grad_batch64.md"},
+}
+
 # kernel function of each timed launch variant (the forward pass and the
 # recompute launch the same function, the recompute with the tape written)
 FUNCTION = {"sort_initial": "dexmpm_sort", "permute_grad_initial": "k_permute", "sort": "dexmpm_sort",
@@ -564,6 +579,8 @@ def roofline(E, kt, cells):
            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of ncu captures of each launch variant on "
                            "the same 64-env batch (654,552 particles, 5 substeps per env step), per particle x n, "
                            "averaged over the variants by launches per substep; profiles/k_<kernel>_batch64.md"}
+    if top in NCU_LIMITER:
+        out["limiter"] = NCU_LIMITER[top]
     red = [NCU_L2_RED[k] for k in variants[top] if k in NCU_L2_RED]
     if red:
         out["atomics"] = {"l2_red_requests_per_launch": int(np.mean([r[0] for r in red])),
