@@ -39,7 +39,7 @@ class DexBatch(ctypes.Structure):
                 ("vol", c_void_p), ("mu_lam_yield", c_void_p), ("grid", c_void_p), ("vout", c_void_p),
                 ("vout_grad", c_void_p), ("in_grad", c_void_p), ("block_flag", c_void_p),
                 ("block_list", c_void_p), ("block_count", c_void_p), ("done_counter", c_void_p),
-                ("body_shape", c_void_p), ("error", c_void_p)]
+                ("body_shape", c_void_p), ("error", c_void_p), ("block_xyz", c_void_p)]
 
 
 class DexSortWork(ctypes.Structure):

@@ -672,12 +672,13 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, i
     v = boundary_forward(v, gxi, gyi, gzi, E.gx, E.gy, E.gz, E.ground_friction);
     return make_float4(v.x, v.y, v.z, __uint_as_float(hit));
   };
-  auto coords = [](const DexEnv &E, int blk, int &bx, int &by, int &bz) {
-    const int local = blk - E.blk_off;
-    const int nby = E.gy >> 2, nbz = E.gz >> 2;
-    bx = local / (nby * nbz);
-    by = (local / nbz) % nby;
-    bz = local % nbz;
+  // the block's coordinates in its env (a table lookup, not three integer
+  // divisions per cell)
+  auto coords = [&](int blk, int &bx, int &by, int &bz) {
+    const int c = B.block_xyz[blk];
+    bx = c >> 20;
+    by = (c >> 10) & 1023;
+    bz = c & 1023;
   };
   const int stride = gridDim.x * per_cta;
   // the list entries of the next two items and the env of the next one are
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_MINB) k_grid_op(DexBatch B, i
     blk_b = item + 2 * stride < cnt ? list[item + 2 * stride] : 0;
     const DexEnv E = B.envs[env];
     int bx, by, bz;
-    coords(E, blk, bx, by, bz);
+    coords(blk, bx, by, bz);
     const int ci = (blk << 6) + cell;
     const float4 g = grid[ci];
     const uint32_t near = bodies_near_block(B, E, pose, bx, by, bz, E.n_bodies);
@@ -901,9 +902,8 @@ __global__ void __launch_bounds__(256, DEX_GRID_OP_GRAD_MINB) k_grid_op_grad(Dex
     const bool in_list = item < cnt;
     const int blk = in_list ? list[item] : 0;
     const DexEnv E = B.envs[B.block_env[blk]];
-    const int local = blk - E.blk_off;
-    const int nby = E.gy >> 2, nbz = E.gz >> 2;
-    const int bx = local / (nby * nbz), by = (local / nbz) % nby, bz = local % nbz;
+    const int c = B.block_xyz[blk];  // the block's coordinates in its env
+    const int bx = c >> 20, by = (c >> 10) & 1023, bz = c & 1023;
     const int gxi = (bx << 2) + (cell >> 4), gyi = (by << 2) + ((cell >> 2) & 3), gzi = (bz << 2) + (cell & 3);
     const int ci = (blk << 6) + cell;
     const float4 g = in_list ? grid[ci] : z4;
@@ -1295,7 +1295,8 @@ __global__ void k_reset_counts(DexBatch B) {
 int check_launch() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
 
 bool valid(const DexBatch *b) {
-  return b && b->envs && b->tiles && b->block_env && b->mass && b->vol && b->mu_lam_yield && b->grid && b->vout &&
+  return b && b->envs && b->tiles && b->block_env && b->block_xyz && b->mass && b->vol && b->mu_lam_yield && b->grid &&
+         b->vout &&
          b->block_flag && b->block_list && b->block_count && b->done_counter && b->error && b->n_tiles >= 0 &&
          b->n_blocks > 0 && b->n_slots > 0 && (b->tile_size == 64 || b->tile_size == 128 || b->tile_size == 256) &&
          b->grid_ctas > 0;

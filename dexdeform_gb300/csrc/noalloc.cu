@@ -39,7 +39,8 @@ constexpr size_t kVout = kGrid0 + (size_t)kMaxCells * 16;
 constexpr size_t kFlag0 = kVout + (size_t)kMaxCells * 16;
 constexpr size_t kList0 = kFlag0 + (size_t)kMaxBlocks * 4;
 constexpr size_t kBlockEnv = kList0 + (size_t)kMaxBlocks * 4;
-constexpr size_t kTiles = kBlockEnv + (size_t)kMaxBlocks * 4;
+constexpr size_t kBlockXyz = kBlockEnv + (size_t)kMaxBlocks * 4;
+constexpr size_t kTiles = kBlockXyz + (size_t)kMaxBlocks * 4;
 constexpr size_t kEnv = kTiles + (size_t)kMaxTiles * 8;
 constexpr size_t kCounts = kEnv + 256;  // block_count, done_counter, error
 constexpr size_t kBytes = kCounts + 256;
@@ -69,12 +70,15 @@ int device_sms() {
 
 bool positive_finite(float v) { return v > 0.f && v <= 3.0e38f; }
 
-// Writes the env descriptor, the tiles and the block->env table, and zeroes
-// the flags, list counts and ticket used by this call.
+// Writes the env descriptor, the tiles and the block tables (owner,
+// coordinates), and zeroes the flags, list counts and ticket used by this
+// call.
 __global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks) {
   unsigned char *base = g_noalloc_scratch;
   int32_t *tiles = reinterpret_cast<int32_t *>(base + kTiles);
   int32_t *block_env = reinterpret_cast<int32_t *>(base + kBlockEnv);
+  int32_t *block_xyz = reinterpret_cast<int32_t *>(base + kBlockXyz);
+  const int nby = env.gy >> 2, nbz = env.gz >> 2;
   uint32_t *flag0 = reinterpret_cast<uint32_t *>(base + kFlag0);
   int stride = gridDim.x * blockDim.x;
   int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -84,6 +88,7 @@ __global__ void k_noalloc_setup(DexEnv env, int n_tiles, int n_blocks) {
   }
   for (int b = t0; b < n_blocks; b += stride) {
     block_env[b] = 0;
+    block_xyz[b] = ((b / (nby * nbz)) << 20) | (((b / nbz) % nby) << 10) | (b % nbz);
     flag0[b] = 0u;
   }
   if (t0 == 0) {
@@ -139,6 +144,7 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   b.envs = reinterpret_cast<const DexEnv *>(base + kEnv);
   b.tiles = reinterpret_cast<const int32_t *>(base + kTiles);
   b.block_env = reinterpret_cast<const int32_t *>(base + kBlockEnv);
+  b.block_xyz = reinterpret_cast<const int32_t *>(base + kBlockXyz);
   b.mass = mass;
   b.vol = vol;
   b.mu_lam_yield = mu_lam_yield;

@@ -125,10 +125,11 @@ class Capacity:
 def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
     """Host-side layout of a batch: particle / block / body offsets per env,
     particle tiles (env, first particle) that never straddle envs, as an
-    (n_tiles, 2) int32 array, the owning env of every grid block (int32), and
-    the DexEnv descriptors."""
+    (n_tiles, 2) int32 array, the owning env of every grid block and its
+    coordinates in that env's grid of 4^3 blocks (bx << 20 | by << 10 | bz,
+    int32), and the DexEnv descriptors."""
     envs = (N.DexEnv * len(specs))()
-    p_off, blk_off, body_off, tiles, nblk = [], [], [], [], []
+    p_off, blk_off, body_off, tiles, nblk, xyz = [], [], [], [], [], []
     p = blk = body = 0
     for e, s in enumerate(specs):
         nbx, nby, nbz = (g // 4 for g in s.grid_dim)
@@ -145,13 +146,18 @@ def plan_layout(specs: Sequence[EnvSpec], tile_size: int) -> dict:
         first = np.arange(0, s.n, tile_size, dtype=np.int32)
         tiles.append(np.stack([np.full_like(first, e), first], 1))
         nblk.append(nbx * nby * nbz)
+        assert max(nbx, nby, nbz) < 1024, "at most 1,023 blocks of 4 cells per axis"
+        bx, by, bz = np.meshgrid(np.arange(nbx, dtype=np.int32), np.arange(nby, dtype=np.int32),
+                                 np.arange(nbz, dtype=np.int32), indexing="ij")
+        xyz.append(((bx << 20) | (by << 10) | bz).reshape(-1))
         p += s.n
         blk += nbx * nby * nbz
         body += s.nb
     tiles = np.concatenate(tiles) if tiles else np.zeros((0, 2), np.int32)
     block_env = np.repeat(np.arange(len(specs), dtype=np.int32), nblk)
-    return dict(envs=envs, tiles=tiles, block_env=block_env, p_off=p_off, blk_off=blk_off, body_off=body_off,
-                n_blocks=blk, n_bodies=body, n_particles=p)
+    block_xyz = np.concatenate(xyz) if xyz else np.zeros(0, np.int32)
+    return dict(envs=envs, tiles=tiles, block_env=block_env, block_xyz=block_xyz, p_off=p_off, blk_off=blk_off,
+                body_off=body_off, n_blocks=blk, n_bodies=body, n_particles=p)
 
 
 class BatchEngine:
@@ -191,6 +197,7 @@ class BatchEngine:
         self.envs_t = torch.zeros(C.envs * ctypes.sizeof(N.DexEnv), dtype=torch.uint8, device=dev)
         self.tiles_t = torch.zeros((C.tiles, 2), **i32)
         self.block_env_t = torch.zeros(C.blocks, **i32)
+        self.block_xyz_t = torch.zeros(C.blocks, **i32)
         # material planes: mass, vol, mu, lambda, yield stress
         self.mat = torch.zeros((MATERIAL_PLANES, self.n_particles), **f32)
         self.mass, self.vol, self.mly = self.mat[0], self.mat[1], self.mat[2:5]
@@ -223,6 +230,7 @@ class BatchEngine:
         b.block_flag, b.block_list = self.block_flag.data_ptr(), self.block_list.data_ptr()
         b.block_count, b.done_counter = self.block_count.data_ptr(), self.done_counter.data_ptr()
         b.body_shape, b.error = self.body_shape.data_ptr(), self.error.data_ptr()
+        b.block_xyz = self.block_xyz_t.data_ptr()
         self.batch = b
         self._bp = ctypes.byref(b)
         self.fslot = 0          # grid slot of the next forward substep (0 or 1)
@@ -260,6 +268,7 @@ class BatchEngine:
             self._upload(self.tiles_t[:len(tiles)], tiles, staged)
         if L["n_blocks"]:
             self._upload(self.block_env_t[:L["n_blocks"]], L["block_env"], staged)
+            self._upload(self.block_xyz_t[:L["n_blocks"]], L["block_xyz"], staged)
         if self.n_bodies:
             shapes = np.zeros((self.n_bodies, 8), np.float32)
             for e, s in enumerate(self.specs):
@@ -285,7 +294,8 @@ class BatchEngine:
 
     def relayout(self, specs: Sequence[EnvSpec], material: bool = True):
         """Move the engine to another set of envs within its capacity: rewrite
-        the env, tile and block tables, the body shapes and (material=True)
+        the env, tile and block tables (owner and coordinates of each block),
+        the body shapes and (material=True)
         the material planes, on the current stream through pinned staging, so
         that the host does not wait.  The grid slots stay: every slot's active
         blocks are cleared by the launch that consumes it, so a slot left in

@@ -209,6 +209,8 @@ typedef struct {
   uint32_t *done_counter;     /* [1] */
   const float *body_shape;    /* [n_bodies][8] */
   int32_t *error;             /* [1] sticky DEXMPM_ERR_* bits */
+  const int32_t *block_xyz;   /* [n_blocks]: the block's coordinates in its env's grid of 4^3
+                                 blocks, bx << 20 | by << 10 | bz (up to 1,023 blocks per axis) */
 } DexBatch;
 
 /* Zero every grid slot, flag, list count and the error word.  Call once after

@@ -35,13 +35,14 @@ def test_struct_layouts_match_header():
         f.write('#include <stdio.h>\n#include <stddef.h>\n#include "dexmpm.h"\nint main(){'
                 'printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(DexEnv), offsetof(DexEnv, gravity), '
                 'sizeof(DexBatch), offsetof(DexBatch, grid), offsetof(DexBatch, block_count), '
-                'offsetof(DexBatch, error), sizeof(DexSortWork), offsetof(DexSortWork, partial)); return 0;}\n')
+                'offsetof(DexBatch, error), sizeof(DexSortWork), offsetof(DexSortWork, partial)); '
+                'printf("%zu\\n", offsetof(DexBatch, block_xyz)); return 0;}\n')
     exe = src[:-2]
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
     got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(N.DexEnv), N.DexEnv.gravity.offset, ctypes.sizeof(N.DexBatch), N.DexBatch.grid.offset,
             N.DexBatch.block_count.offset, N.DexBatch.error.offset, ctypes.sizeof(N.DexSortWork),
-            N.DexSortWork.partial.offset]
+            N.DexSortWork.partial.offset, N.DexBatch.block_xyz.offset]
     assert got == want
 
 
@@ -250,6 +251,14 @@ def test_layout_plan_and_footprint():
         assert (seen == 1).all()
         assert len(L["block_env"]) == sum((s.grid_dim[0] // 4) ** 3 for s in specs)
         assert all(L["block_env"][L["blk_off"][e]] == e for e in range(len(specs)))
+        # block coordinates: the block index within the env decomposes as
+        # (bx * nby + by) * nbz + bz
+        xyz = L["block_xyz"]
+        for e, sp in enumerate(specs):
+            nby, nbz = sp.grid_dim[1] // 4, sp.grid_dim[2] // 4
+            local = np.arange(len(xyz))[L["block_env"] == e] - L["blk_off"][e]
+            c = xyz[L["block_env"] == e]
+            assert (((c >> 20) * nby + ((c >> 10) & 1023)) * nbz + (c & 1023) == local).all()
     a = footprint_bytes(specs)
     b = footprint_bytes(specs, grad=True, substeps=50, env_steps=10)
     assert 0 < a < b
