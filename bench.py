@@ -763,14 +763,15 @@ def plain_rates(envs, dev, sample_every=8, backend="reference"):
             # MPMSimulator.step: the env step's substeps as one fused sequence
             sim.action_scales = np.full((env.nb, 6), 0.01, np.float32)
             act = np.zeros((env.nb, 6), np.float32)
-            sim.step(act)
+            for _ in range(2):  # both orders of the states (the step swaps two), each captured once
+                sim.step(act)
             torch.cuda.synchronize()
             a.record()
-            for _ in range(2):
+            for _ in range(4):
                 sim.step(act)
             b.record()
             torch.cuda.synchronize()
-            step_t += a.elapsed_time(b) / 2e3
+            step_t += a.elapsed_time(b) / 4e3
         del sim
     out = {"fwd": work / fwd_t, "fwd_bwd": work / bwd_t, "unit": UNIT,
            "what": f"reference schedule through MPMSimulator (backend {backend!r}), one env at a time, "

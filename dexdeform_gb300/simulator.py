@@ -66,6 +66,14 @@ class DeviceArray:
     def __init__(self, shape, dtype=torch.float32, device="cuda"):
         self.t = torch.zeros(shape, dtype=dtype, device=device)
 
+    @classmethod
+    def of(cls, tensor: torch.Tensor) -> "DeviceArray":
+        """A DeviceArray over an existing contiguous tensor (a view)."""
+        assert tensor.is_contiguous()
+        a = cls.__new__(cls)
+        a.t = tensor
+        return a
+
     @property
     def data_ptr(self):
         return ctypes.c_void_p(self.t.data_ptr())
@@ -233,7 +241,9 @@ class SoAState(State):
         self.F_grad, self.C_grad = P(self.gslot[6:15], (n, 3, 3)), P(self.gslot[15:24], (n, 3, 3))
         nb = max(sim.n_bodies, 1)
         A = DeviceArray
-        self.body_pos, self.body_rot = A((nb, 3)), A((nb, 4))
+        # rows of the simulator's pose tables, so that an env step writes the
+        # poses of all its substeps in one copy
+        self.body_pos, self.body_rot = A.of(sim._bpos[index]), A.of(sim._brot[index])
         self.body_pos_grad, self.body_rot_grad = A((nb, 3)), A((nb, 4))
 
 
@@ -274,8 +284,12 @@ class MPMSimulator:
             stride = max(32, (self.n_particles + 31) // 32 * 32)
             self._soa = torch.zeros((max_steps, N.STATE_PLANES, stride), device="cuda")
             self._soa_grad = torch.zeros_like(self._soa)
-            self.states = [SoAState(self, i) for i in range(max_steps)]
             nb = max(n_bodies, 1)
+            self._bpos = torch.zeros((max_steps, nb, 3), device="cuda")
+            self._brot = torch.zeros((max_steps, nb, 4), device="cuda")
+            self._graphs = {}
+            self._row_index = {}
+            self.states = [SoAState(self, i) for i in range(max_steps)]
             self._pose = torch.zeros((substeps + 1, nb, 8), device="cuda")
             self._bgrad = torch.zeros((2, nb, 8), device="cuda")
             self._E = None  # batched engine, built on first use (material and bodies are set after __init__)
@@ -304,6 +318,7 @@ class MPMSimulator:
         is rebuilt on its next use."""
         if getattr(self, "backend", "reference") == "batched":
             self._E = None
+            self._graphs = {}
 
     def _engine(self):
         """One-env BatchEngine over the SoA storage (plane stride of
@@ -627,14 +642,29 @@ class MPMSimulator:
         """mpm/simulator.py:626-634 (batched backend: the env step's substeps
         in one fused sequence, each G2P fused with the next P2G)."""
         pos, rot, _ = self.compute_forward_kinematics(self.cur, action, pos_rot=pos_rot)
-        for f in range(self.substeps):
-            self.set_pose(self.states[f + 1], pos[f], rot[f])
         if self.backend == "batched":
-            T = self.substeps
-            for f in range(T + 1):
-                self._pack_pose(self.states[f], self._pose[f])
-            self._engine().run_substeps([self.states[f].slot for f in range(T + 1)], self._pose[:T + 1])
+            # the substeps' poses into their states' rows in one copy each, the
+            # engine's pose table gathered from the rows, and the env step's
+            # launches replayed as a CUDA graph (one per order of the states,
+            # which the swap below alternates)
+            T, nb = self.substeps, self.n_bodies
+            rows = tuple(self.states[f].index for f in range(T + 1))
+            idx = self._row_index.get(rows)
+            if idx is None:
+                idx = self._row_index[rows] = torch.tensor(rows, device="cuda")
+            if nb:
+                f32 = dict(dtype=torch.float32, device="cuda")
+                self._bpos.index_copy_(0, idx[1:], torch.as_tensor(pos).to(**f32).reshape(T, nb, 3))
+                self._brot.index_copy_(0, idx[1:], torch.as_tensor(rot).to(**f32).reshape(T, nb, 4))
+                self._pose[:T + 1, :nb, :3] = self._bpos.index_select(0, idx)[:, :nb]
+                self._pose[:T + 1, :nb, 4:] = self._brot.index_select(0, idx)[:, :nb]
+            from .engine import run_graph
+            E = self._engine()
+            slots = [self.states[f].slot for f in range(T + 1)]
+            run_graph(E, self._graphs, ("step", rows), lambda: E.run_substeps(slots, self._pose[:T + 1]))
         else:
+            for f in range(self.substeps):
+                self.set_pose(self.states[f + 1], pos[f], rot[f])
             for f in range(self.substeps):
                 self.substep(f)
         self.sync()

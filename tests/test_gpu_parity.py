@@ -195,6 +195,38 @@ def test_simulator_batched_backend_equals_engine(cuda):
         assert sim._engine().error_word() == 0
 
 
+def test_simulator_step_equals_substep_loop(cuda):
+    """MPMSimulator.step on the batched backend (the substeps' poses written in
+    one copy, the env step replayed as a CUDA graph, one per order of the
+    states, which each step swaps) over 4 env steps under random actions:
+    the particle state and the body poses after every step equal those of the
+    reference's schedule (set_pose and substep per substep, then the same
+    swap), up to float-atomic ordering (1e-4) and FP32 rounding (1e-6)."""
+    from dexdeform_gb300 import workloads as W
+    T = 10
+    env = W.make_env(12, 3000, "cube", grid=64, center=(0.5, 0.15, 0.5), extent=0.2, nb=6, steps=T, sort=False)
+    rng = np.random.default_rng(0)
+    acts = rng.uniform(-1, 1, (4, env.nb, 6)).astype(np.float32)
+    a, b = _abi_sim(env, T, "batched"), _abi_sim(env, T, "batched")
+    for sim in (a, b):
+        sim.action_scales = np.full((env.nb, 6), 0.02, np.float32)
+    for k in range(4):
+        a.step(acts[k])
+        pos, rot, _ = b.compute_forward_kinematics(b.cur, acts[k])
+        for f in range(T):
+            b.set_pose(b.states[f + 1], pos[f], rot[f])
+        for f in range(T):
+            b.substep(f)
+        b.states[0], b.states[T] = b.states[T], b.states[0]
+        sa, sb = a.get_state(0), b.get_state(0)
+        for i in range(4):
+            assert rel(sa[i], sb[i]) < 1e-4, (k, i)
+        assert max(np.abs(np.asarray(p) - np.asarray(q)).max() for p, q in zip(sa[4:], sb[4:])) < 1e-6, k
+        for f in range(1, T):  # the intermediate states carry their substep's poses too
+            assert np.allclose(a.states[f].body_pos.download(), b.states[f].body_pos.download(), atol=1e-6)
+    assert a._engine().error_word() == 0 and len(a._graphs) == 2
+
+
 @pytest.mark.parametrize("backend", ["reference", "batched"])
 def test_reference_abi_adjoint(cuda, oracle_mod, backend):
     env, z = golden_env(os.path.join(GOLDEN, "ref_grad_32.npz"))
