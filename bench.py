@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation (config 1) leg")
     ap.add_argument("--no-overlap", action="store_true",
                     help="backward without recomputing env step k - 1 on a second stream during the adjoint of k")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
@@ -317,6 +318,7 @@ def run_ours(args, rank, world, local):
     serving_sat = None if (args.no_serving or world > 1) else serving_leg(dev, seed=rank, n_req=args.serving_requests,
                                                                          rate_hz=60.0)
     large = None if (args.no_large or world > 1) else large_env_leg(dev)
+    diff = None if (args.no_diff or world > 1) else differentiation_leg(dev)
     rend = None if (args.no_render or world > 1) else render_leg(dev, cpu=not args.no_cpu)
 
     if rank == 0:
@@ -361,6 +363,8 @@ def run_ours(args, rank, world, local):
             out["serving_saturated"] = serving_sat
         if large is not None:
             out["large_env"] = large
+        if diff is not None:
+            out["differentiation"] = diff
         if rend is not None:
             out["render"] = rend
         out["clocks"] = clk.summary()
@@ -623,6 +627,59 @@ def serving_leg(dev, seed=0, n_req=200, rate_hz=20.0):
             "hbm_budget_gb": 180, "what": "Poisson arrivals, 48/64/96^3 grids, 2k-50k particles in sampling order "
                                           "(sorted by grid cell on the device each round), horizons 5-100 env "
                                           "steps x 50 substeps, 30% gradient requests; continuous batching"}
+
+
+def differentiation_leg(dev, env_steps=20, substeps=50):
+    """The differentiation form on config 1 through the autograd path
+    (torch_wrapper.GradModel): 20,000 particles in an ellipsoid, a 24-joint
+    hand of 22 capsules driven by 24 joint-velocity controls N(0, 0.1) for 20
+    env steps x 50 substeps, checkpoint per env step, loss = mean squared
+    distance to a seeded target cloud; loss.backward() gives the gradients
+    wrt every control and the initial state.  Whole rollouts (forward, loss,
+    backward) timed with CUDA events after two warm-up rollouts."""
+    import torch
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.hand import N_BODIES, SyntheticHand, default_qpos
+    from dexdeform_gb300.torch_wrapper import GradModel
+    hand = SyntheticHand(base_pos=(0.5, 0.2, 0.47), action_scale=0.05)
+    env = W.make_env(11, 20000, "ellipsoid", grid=64, dt=5e-5, center=(0.5, 0.11, 0.5), extent=(0.12, 0.06, 0.09),
+                     nb=N_BODIES, steps=2, sort=False, name="config1")
+    env.body_tfsr, env.body_args = hand.body_shapes()
+    rng = np.random.default_rng(0)
+    actions = torch.tensor(rng.normal(scale=0.1, size=(env_steps, 24)), dtype=torch.float32, device=dev)
+    target = torch.tensor(env.x + rng.normal(scale=0.01, size=env.x.shape).astype(np.float32), device=dev)
+    model = GradModel(env, hand, substeps)
+    q0 = default_qpos()
+    s0 = model.sim.E.pack_state([env.state()])
+
+    def rollout():
+        a = actions.clone().requires_grad_(True)
+        st = s0.clone().requires_grad_(True)
+        model.zero_grad()
+        model.reset(q0, st)
+        for k in range(env_steps):
+            obs = model.forward(k, a[k])
+        loss = ((obs[0][:, :3] - target) ** 2).sum(1).mean()
+        loss.backward()
+        return a.grad
+
+    for _ in range(2):
+        rollout()
+    torch.cuda.synchronize()
+    reps = 3
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    for _ in range(reps):
+        g = rollout()
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / reps
+    assert model.sim.E.error_word() == 0 and bool(torch.isfinite(g).all())
+    work = env.n * env_steps * substeps
+    return {"value": work / (ms * 1e-3), "unit": UNIT, "ms_per_rollout": round(ms, 3),
+            "what": "config 1 through GradModel: 20,000 particles (sampling order, sorted on the device each env "
+                    "step), 24 joint-velocity controls x 20 env steps x 50 substeps, 22 capsules, forward + loss + "
+                    "backward to every control and the initial state"}
 
 
 def large_env_leg(dev, substeps=100, env_steps=10):

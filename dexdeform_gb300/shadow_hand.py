@@ -161,6 +161,14 @@ def axis_angle_to_matrix(v: torch.Tensor) -> torch.Tensor:
     return eye + a[..., None, None] * K + b[..., None, None] * (K @ K)
 
 
+def homogeneous_row(like: torch.Tensor, lead) -> torch.Tensor:
+    """The bottom row (0, 0, 0, 1) of homogeneous matrices, shaped lead + (1,
+    4), made on like's device (no host copy, so that it can be captured in a
+    CUDA graph)."""
+    row = (torch.arange(4, device=like.device) == 3).to(like.dtype)
+    return row.expand(tuple(lead) + (1, 4))
+
+
 def quaternion_to_matrix(q: torch.Tensor) -> torch.Tensor:
     """(..., 4) quaternions w, x, y, z (any norm) -> (..., 3, 3) rotations."""
     w, x, y, z = q.unbind(-1)
@@ -450,8 +458,7 @@ class ShadowHand:
         (..., 24, 4, 4) joint frames."""
         R = axis_angle_to_matrix(self.axis * q[..., None])            # (..., 24, 3, 3)
         T = torch.cat([torch.cat([R, self.p.expand(R.shape[:-1])[..., None]], -1),
-                       torch.tensor([0.0, 0.0, 0.0, 1.0], dtype=R.dtype, device=R.device).expand(
-                           R.shape[:-2] + (1, 4))], -2)                   # (..., 24, 4, 4)
+                       homogeneous_row(R, R.shape[:-2])], -2)           # (..., 24, 4, 4)
         frames: List[Optional[torch.Tensor]] = [None] * len(JOINTS)
         for j in self._order:
             par = self.model.parent[j]
@@ -485,8 +492,7 @@ class ShadowHand:
         out = out / torch.linalg.norm(out, dim=-1, keepdim=True)
         R = quaternion_to_matrix(out)
         top = torch.cat([R, pos[..., None]], -1)
-        bottom = torch.tensor([0.0, 0.0, 0.0, 1.0], dtype=base.dtype, device=base.device).expand(top.shape[:-2] + (1, 4))
-        return torch.cat([top, bottom], -2)
+        return torch.cat([top, homogeneous_row(base, top.shape[:-2])], -2)
 
     def joint_velocity_fk(self, base: torch.Tensor, q: torch.Tensor, actions: torch.Tensor, substeps: int):
         """mpm/hand.py:383-428 (JointVel_Fk): actions (H, 20) joint velocities

@@ -211,7 +211,15 @@ class GradModel:
     (particles (n, 6 + nb) = x | v | distances to every body, tool state
     (nb, 7), and the grid mass when return_grid is set).  loss.backward()
     runs the adjoint through every env step (set_obs_grad is what autograd
-    does with the observation gradients)."""
+    does with the observation gradients).
+
+    With use_graphs the hand's kinematics of each env step (a few hundred
+    small tensor operations forward and as many backward) run as CUDA graphs
+    (torch.cuda.make_graphed_callables), one per env step index and
+    requires-grad pattern of its inputs; the MPM env steps replay their own
+    graphs in DiffSim.  A graphed step's outputs live in its graph's memory:
+    run a rollout's backward before the next rollout's forward reaches that
+    env step again (the reference's training loop does)."""
 
     def __init__(self, env, hand, substeps, return_grid=(), device="cuda", use_graphs=True,
                  capsule_grad="reference", sort=True):
@@ -227,6 +235,8 @@ class GradModel:
         self.mass = torch.tensor(env.mass, device=self.device)
         self.return_grid = tuple(return_grid)
         self.substeps = substeps
+        self.use_graphs = use_graphs and self.device.type == "cuda"
+        self._fk_graphs = {}
         self.zero_grad()
 
     def zero_grad(self, return_grid=None, **kw):
@@ -259,9 +269,28 @@ class GradModel:
             out.append(grid_mass(x.contiguous(), self.mass, self.env.grid_dim, self.env.dx))
         return tuple(out)
 
+    def _joint_velocity_poses(self, s, q, action):
+        """Poses of the env step's substeps (substeps, nb, 8) and the final
+        joint angles, through the hand's joint-velocity kinematics."""
+        T = self.substeps
+
+        def fk(q, a):
+            pos, rot, q_last = self.hand.joint_velocity_poses(q, a, T)
+            return pack_pose_tensor(pos, rot), q_last
+
+        if not (self.use_graphs and torch.is_grad_enabled() and (q.requires_grad or action.requires_grad)):
+            return fk(q, action)  # no gradient wanted: plain forward
+        key = (s, q.requires_grad, action.requires_grad)
+        g = self._fk_graphs.get(key)
+        if g is None:
+            sample = (q.detach().clone().requires_grad_(q.requires_grad),
+                      action.detach().clone().requires_grad_(action.requires_grad))
+            g = self._fk_graphs[key] = torch.cuda.make_graphed_callables(fk, sample)
+        return g(q, action)
+
     def forward(self, s, action, *past_obs):
-        pos, rot, q_last = self.hand.joint_velocity_poses(self.qpos, action, self.substeps)
-        poses = torch.cat([self.last_pose[None], pack_pose_tensor(pos, rot)], 0)
+        packed, q_last = self._joint_velocity_poses(s, self.qpos, action)
+        poses = torch.cat([self.last_pose[None], packed], 0)
         self.state = env_step(self.sim, self.state, poses)
         self.qpos = q_last
         self.last_pose = poses[-1]

@@ -291,3 +291,53 @@ def test_config1_full_size_gradients(cuda):
     assert np.median(err) < 0.1, (fd, an)
     assert abs(fd_dir - g_dir) < 0.1 * abs(g_dir), (fd_dir, g_dir)
     assert (err < 0.25).sum() >= 10, (fd, an)
+
+
+@pytest.mark.parametrize("hand_kind", ["synthetic", "shadow"])
+def test_graphed_kinematics_equal_eager(cuda, hand_kind):
+    """GradModel with the hand kinematics of each env step replayed as CUDA
+    graphs gives the loss and the control and initial-state gradients of the
+    eager model, over two rollouts (the second replays every graph); the MPM
+    part differs only by float-atomic ordering (states 2e-4, gradients
+    5e-4)."""
+    import os
+    from conftest import GOLDEN
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.torch_wrapper import GradModel
+    if hand_kind == "synthetic":
+        from dexdeform_gb300.hand import N_BODIES, SyntheticHand, default_qpos
+        hand, nb, n_act, q0 = SyntheticHand(base_pos=(0.5, 0.2, 0.47), action_scale=0.05), N_BODIES, 24, default_qpos()
+    else:
+        from dexdeform_gb300.shadow_hand import DEFAULT_INITIAL_QPOS, HandModel, ShadowHand, root_matrix
+        model = HandModel.load(os.path.join(GOLDEN, "shadow_rh_model.npz")).scaled(2.5)
+        hand = ShadowHand(model, device="cuda", action_scale=np.full(26, 0.02)).set_base(
+            root_matrix((0.5, 0.16, 0.3), (0.0, 0.0, 0.0)))
+        nb, n_act = 19, 26
+        q0 = torch.tensor(DEFAULT_INITIAL_QPOS, dtype=torch.float32, device="cuda")
+    env = W.make_env(5, 3000, "ellipsoid", grid=64, dt=5e-5, center=(0.5, 0.11, 0.5), extent=(0.12, 0.06, 0.09),
+                     nb=nb, steps=1, sort=False)
+    env.body_tfsr, env.body_args = hand.body_shapes()
+    S, T = 3, 10
+    rng = np.random.default_rng(1)
+    actions = torch.tensor(rng.normal(scale=0.3, size=(S, n_act)), dtype=torch.float32, device="cuda")
+    target = torch.tensor(env.x + rng.normal(scale=0.01, size=env.x.shape).astype(np.float32), device="cuda")
+    res = []
+    for graphs in (False, True):
+        model = GradModel(env, hand, T, use_graphs=graphs, capsule_grad="exact")
+        s0 = model.sim.E.pack_state([W.perturb_state(env, seed=2, v_scale=0.1, c_scale=1.0, f_scale=0.02)])
+        for _ in range(2):
+            a = actions.clone().requires_grad_(True)
+            st = s0.clone().requires_grad_(True)
+            model.zero_grad()
+            model.reset(q0, st)
+            for k in range(S):
+                obs = model.forward(k, a[k])
+            loss = ((obs[0][:, :3] - target) ** 2).sum(1).mean()
+            loss.backward()
+        assert model.sim.E.error_word() == 0
+        res.append((float(loss), a.grad.clone(), st.grad.clone(), obs[1].detach().clone()))
+    (l0, ga0, gs0, p0), (l1, ga1, gs1, p1) = res
+    assert abs(l1 - l0) <= 2e-4 * abs(l0)
+    assert torch.equal(p0, p1)  # the hand's poses: the same kernels, no atomics
+    assert rel(ga1.cpu().numpy(), ga0.cpu().numpy()) < 5e-4
+    assert rel(gs1.cpu().numpy(), gs0.cpu().numpy()) < 5e-4
