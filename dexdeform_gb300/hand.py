@@ -63,24 +63,53 @@ N_BODIES = len(_C)
 assert N_BODIES == 22
 
 
-def _qmul(a, b):
-    aw, ax, ay, az = a.unbind(-1)
-    bw, bx, by, bz = b.unbind(-1)
-    return torch.stack([aw * bw - ax * bx - ay * by - az * bz, aw * bx + ax * bw + ay * bz - az * by,
-                        aw * by - ax * bz + ay * bw + az * bx, aw * bz + ax * by - ay * bx + az * bw], -1)
+# The joints by depth in the tree: every joint of a level has its parent in
+# an earlier level, so a level's joints are placed together.
+def _levels():
+    depth = []
+    for name, parent, *_ in _J:
+        depth.append(0 if parent < 0 else depth[parent] + 1)
+    return [[j for j in range(len(_J)) if depth[j] == d] for d in range(max(depth) + 1)]
 
 
-def _qrot(q, v):
-    qv = q[..., 1:]
-    uv = torch.cross(qv, v, dim=-1)
-    uuv = torch.cross(qv, uv, dim=-1)
-    return v + 2.0 * (q[..., :1] * uv + uuv)
+def _hamilton():
+    """H with (a b)_i = sum_jk H[i, j, k] a_j b_k for quaternions w, x, y, z."""
+    H = torch.zeros(4, 4, 4)
+    for i, j, k, s in ((0, 0, 0, 1), (0, 1, 1, -1), (0, 2, 2, -1), (0, 3, 3, -1),
+                       (1, 0, 1, 1), (1, 1, 0, 1), (1, 2, 3, 1), (1, 3, 2, -1),
+                       (2, 0, 2, 1), (2, 1, 3, -1), (2, 2, 0, 1), (2, 3, 1, 1),
+                       (3, 0, 3, 1), (3, 1, 2, 1), (3, 2, 1, -1), (3, 3, 0, 1)):
+        H[i, j, k] = s
+    return H
 
 
-def _axis_angle(axis, angle):
-    axis = axis / torch.linalg.norm(axis)
-    h = angle[..., None] * 0.5
-    return torch.cat([torch.cos(h), torch.sin(h) * axis], -1)
+def _rotation_form():
+    """R with rot(q)_ij = sum_kl R[i, j, k, l] q_k q_l for unit quaternions
+    (the identity part of the rotation matrix written as |q|^2)."""
+    R = torch.zeros(3, 3, 4, 4)
+    w, x, y, z = 0, 1, 2, 3
+    def put(i, j, terms):
+        for k, l, s in terms:
+            R[i, j, k, l] += s
+    put(0, 0, ((w, w, 1), (x, x, 1), (y, y, -1), (z, z, -1)))
+    put(1, 1, ((w, w, 1), (x, x, -1), (y, y, 1), (z, z, -1)))
+    put(2, 2, ((w, w, 1), (x, x, -1), (y, y, -1), (z, z, 1)))
+    put(0, 1, ((x, y, 2), (w, z, -2)))
+    put(0, 2, ((x, z, 2), (w, y, 2)))
+    put(1, 0, ((x, y, 2), (w, z, 2)))
+    put(1, 2, ((y, z, 2), (w, x, -2)))
+    put(2, 0, ((x, z, 2), (w, y, -2)))
+    put(2, 1, ((y, z, 2), (w, x, 2)))
+    return R
+
+
+def _qmul(H, a, b):
+    return torch.einsum("ijk,...j,...k->...i", H, a, b)
+
+
+def _qrot(R, q, v):
+    """Rotate v by the unit quaternion q."""
+    return torch.einsum("ijkl,...k,...l,...j->...i", R, q, q, v)
 
 
 class SyntheticHand:
@@ -102,6 +131,21 @@ class SyntheticHand:
         self.base_pos = torch.tensor(base_pos, **f)
         self.base_rot = torch.tensor(base_rot, **f)
         self.action_scale = action_scale
+        self.H, self.R = _hamilton().to(**f), _rotation_form().to(**f)
+        self.unit_axes = self.axes / torch.linalg.norm(self.axes, dim=-1, keepdim=True)
+        # per level: its joints, and where each one's parent sits in the
+        # running table of world poses (row 0 the base, then the levels in order)
+        row = {}
+        self.level_joints, self.level_parent_rows = [], []
+        n = 1
+        for js in _levels():
+            self.level_joints.append(torch.tensor(js, dtype=torch.long, device=self.device))
+            self.level_parent_rows.append(torch.tensor([0 if _J[j][1] < 0 else row[_J[j][1]] for j in js],
+                                                       dtype=torch.long, device=self.device))
+            for j in js:
+                row[j] = n
+                n += 1
+        self.cap_rows = torch.tensor([row[j] for j in self.cap_joint], dtype=torch.long, device=self.device)
 
     def body_shapes(self):
         """(22, 4) type friction softness round, (22, 4) args (radius, length)."""
@@ -115,21 +159,23 @@ class SyntheticHand:
         return tfsr, args
 
     def fk(self, q):
-        """q (..., 24) -> pos (..., 22, 3), rot (..., 22, 4)."""
+        """q (..., 24) -> pos (..., 22, 3), rot (..., 22, 4).  Joint j's world
+        frame is its parent's composed with the joint's offset (translation
+        origin_j in the parent frame) and rotation (angle q_j about axis_j);
+        a capsule sits at an offset in its joint's frame.  The joints of one
+        depth of the tree are done together."""
         lead = q.shape[:-1]
-        qs = [None] * len(_J)
-        ps = [None] * len(_J)
-        base_q = self.base_rot.expand(*lead, 4)
-        base_p = self.base_pos.expand(*lead, 3)
-        for j, (name, parent, axis, origin, lo, hi) in enumerate(_J):
-            pq = base_q if parent < 0 else qs[parent]
-            pp = base_p if parent < 0 else ps[parent]
-            ps[j] = pp + _qrot(pq, self.origins[j].expand(*lead, 3))
-            qs[j] = _qmul(pq, _axis_angle(self.axes[j], q[..., j]))
-        pos = torch.stack([ps[j] + _qrot(qs[j], self.cap_off[c].expand(*lead, 3))
-                           for c, j in enumerate(self.cap_joint)], -2)
-        rot = torch.stack([qs[j] for j in self.cap_joint], -2)
-        return pos, rot
+        Q = self.base_rot.expand(*lead, 1, 4)   # world rotations, row 0 the base
+        P = self.base_pos.expand(*lead, 1, 3)   # world positions
+        for js, rows in zip(self.level_joints, self.level_parent_rows):
+            pq, pp = Q.index_select(-2, rows), P.index_select(-2, rows)
+            h = q.index_select(-1, js)[..., None] * 0.5
+            local = torch.cat([torch.cos(h), torch.sin(h) * self.unit_axes[js]], -1)
+            P = torch.cat([P, pp + _qrot(self.R, pq, self.origins[js].expand(pq.shape[:-1] + (3,)))], -2)
+            Q = torch.cat([Q, _qmul(self.H, pq, local)], -2)
+        cq, cp = Q.index_select(-2, self.cap_rows), P.index_select(-2, self.cap_rows)
+        pos = cp + _qrot(self.R, cq, self.cap_off.expand(cq.shape[:-1] + (3,)))
+        return pos, cq
 
     def joint_velocity_poses(self, q0, action, substeps):
         """mpm/hand.py:383-428 for a fixed base: q_k = clamp(q0 + a*scale*(k+1)),
