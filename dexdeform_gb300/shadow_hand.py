@@ -412,6 +412,25 @@ class ShadowHand:
         self.G = torch.tensor(model.G, **f)
         self.geom_joint = torch.tensor(model.geom_joint, dtype=torch.long, device=self.device)
         self._order = model.order()
+        # the joints by depth in the tree, each level with the rows of its
+        # parents in the running table of frames (row 0 the base, then the
+        # levels in order), and each joint's row at the end
+        depth = {}
+        for j in self._order:
+            par = int(model.parent[j])
+            depth[j] = 0 if par < 0 else depth[par] + 1
+        row, n = {}, 1
+        self._levels = []
+        for d in range(max(depth.values()) + 1):
+            js = [j for j in self._order if depth[j] == d]
+            rows = [0 if model.parent[j] < 0 else row[int(model.parent[j])] for j in js]
+            self._levels.append((torch.tensor(js, dtype=torch.long, device=self.device),
+                                 torch.tensor(rows, dtype=torch.long, device=self.device),
+                                 torch.tensor([int(model.parent[j]) >= 0 for j in js], device=self.device)))
+            for j in js:
+                row[j] = n
+                n += 1
+        self._rows = torch.tensor([row[j] for j in range(len(JOINTS))], dtype=torch.long, device=self.device)
         lo, hi = joint_limits()
         self.lower, self.upper = torch.tensor(lo, **f), torch.tensor(hi, **f)
         self.action_map = torch.tensor(actuator_of_joint(), dtype=torch.long, device=self.device)
@@ -459,12 +478,14 @@ class ShadowHand:
         R = axis_angle_to_matrix(self.axis * q[..., None])            # (..., 24, 3, 3)
         T = torch.cat([torch.cat([R, self.p.expand(R.shape[:-1])[..., None]], -1),
                        homogeneous_row(R, R.shape[:-2])], -2)           # (..., 24, 4, 4)
-        frames: List[Optional[torch.Tensor]] = [None] * len(JOINTS)
-        for j in self._order:
-            par = self.model.parent[j]
-            src = base if par < 0 else frames[par] @ self.M[j]
-            frames[j] = src @ T[..., j, :, :]
-        return torch.stack(frames, -3)
+        # joint j's frame: its parent's frame @ M_j @ T_j, or base @ T_j at
+        # the root; the joints of one depth of the tree are done together
+        frames = base[..., None, :, :]                                  # (..., 1, 4, 4), row 0 the base
+        for js, rows, has_parent in self._levels:
+            src = frames.index_select(-3, rows)
+            src = torch.where(has_parent[:, None, None], src @ self.M[js], src)
+            frames = torch.cat([frames, src @ T.index_select(-3, js)], -3)
+        return frames.index_select(-3, self._rows)
 
     def forward_kinematics(self, base: torch.Tensor, q: torch.Tensor):
         """mpm/hand.py:347-381: base (S, H, 4, 4), q (S, H, 24) -> geom
