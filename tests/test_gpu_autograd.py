@@ -335,7 +335,7 @@ def test_graphed_kinematics_equal_eager(cuda, hand_kind):
             loss = ((obs[0][:, :3] - target) ** 2).sum(1).mean()
             loss.backward()
         assert model.sim.E.error_word() == 0
-        res.append((float(loss), a.grad.clone(), st.grad.clone(), obs[1].detach().clone()))
+        res.append((float(loss.detach()), a.grad.clone(), st.grad.clone(), obs[1].detach().clone()))
     (l0, ga0, gs0, p0), (l1, ga1, gs1, p1) = res
     assert abs(l1 - l0) <= 2e-4 * abs(l0)
     assert torch.equal(p0, p1)  # the hand's poses: the same kernels, no atomics
