@@ -42,6 +42,14 @@ class DexBatch(ctypes.Structure):
                 ("body_shape", c_void_p), ("error", c_void_p), ("block_xyz", c_void_p)]
 
 
+class DexSegment(ctypes.Structure):
+    _fields_ = [("other", c_void_p), ("other_stride", c_int32), ("offset", c_int32), ("count", c_int32),
+                ("pad", c_int32)]
+
+
+SEGMENTS_GATHER, SEGMENTS_SCATTER, SEGMENTS_SCATTER_ADD = 0, 1, 2
+
+
 class DexSortWork(ctypes.Structure):
     _fields_ = [("cell_count", c_void_p), ("cell_start", c_void_p), ("block_total", c_void_p),
                 ("block_base", c_void_p), ("block_flag", c_void_p), ("block_list", c_void_p), ("rank", c_void_p),
@@ -89,6 +97,7 @@ _BATCH_SIGS = {
     "dexmpm_substep_noalloc": [POINTER(DexEnv), P, P, P, P, P, P, P, P, P, P],
     "dexmpm_sort": [POINTER(DexBatch), POINTER(DexSortWork), P, P, P, P],
     "dexmpm_permute": [P, P, P, c_int, c_int, c_int, P],
+    "dexmpm_copy_segments": [P, c_int, c_int, P, c_int, c_int, c_int, P],
     "dexmpm_abi_get_error": [POINTER(c_int32)],
 }
 

@@ -369,6 +369,25 @@ __global__ void __launch_bounds__(256) k_permute(const int32_t *__restrict__ per
   }
 }
 
+// Segmented plane copy: blockIdx.y = segment, x-threads over its columns,
+// each thread all planes of its column.
+__global__ void __launch_bounds__(256) k_copy_segments(const DexSegment *__restrict__ seg, int planes,
+                                                       float *__restrict__ buf, int buf_stride, int mode) {
+  const DexSegment s = seg[blockIdx.y];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.count; i += gridDim.x * blockDim.x) {
+    for (int q = 0; q < planes; ++q) {
+      float *o = s.other + (size_t)q * s.other_stride + i;
+      float *b = buf + (size_t)q * buf_stride + s.offset + i;
+      if (mode == DEXMPM_SEGMENTS_GATHER)
+        *b = *o;
+      else if (mode == DEXMPM_SEGMENTS_SCATTER)
+        *o = *b;
+      else
+        *o += *b;
+    }
+  }
+}
+
 int check_launch() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
 
 int device_sms() {
@@ -419,6 +438,19 @@ int dexmpm_sort(const DexBatch *b, const DexSortWork *w, const float *s, float *
   k_sort_fix_big<<<persistent, 256, 0, st>>>(*w, perm);
   if (int rc = check_launch()) return rc;
   return dexmpm_permute(perm, s, sorted_s, b->n_particles, DEXMPM_STATE_PLANES, 0, stream);
+}
+
+int dexmpm_copy_segments(const DexSegment *seg, int n, int planes, float *buf, int buf_stride, int mode,
+                         int max_count, dexmpm_stream_t stream) {
+  if (n < 0 || planes < 0 || max_count < 0 || buf_stride < 0 || n > 65535 || mode < DEXMPM_SEGMENTS_GATHER ||
+      mode > DEXMPM_SEGMENTS_SCATTER_ADD)
+    return DEXMPM_ERR_ARG;
+  if (n == 0 || planes == 0 || max_count == 0) return DEXMPM_OK;
+  if (!seg || !buf) return DEXMPM_ERR_ARG;
+  const int per_seg = (max_count + 255) / 256;
+  const dim3 grid(per_seg < 64 ? per_seg : 64, n);
+  k_copy_segments<<<grid, 256, 0, (cudaStream_t)stream>>>(seg, planes, buf, buf_stride, mode);
+  return check_launch();
 }
 
 int dexmpm_permute(const int32_t *perm, const void *src, void *dst, int n, int planes, int inverse,

@@ -35,7 +35,28 @@ from typing import Dict, List, Optional
 import numpy as np
 import torch
 
+from . import _native as N
 from .engine import BatchEngine, Capacity, EnvSpec, footprint_bytes, pack_poses, run_graph
+
+# one DexSegment (include/dexmpm.h)
+_SEGMENT = np.dtype([("other", "<u8"), ("other_stride", "<i4"), ("offset", "<i4"), ("count", "<i4"),
+                     ("pad", "<i4")])
+
+
+def copy_segments(blocks, planes: int, buf: torch.Tensor, buf_stride: int, mode: int):
+    """Copy many blocks of `planes` planes between their own tensors and one
+    shared buffer in one launch (dexmpm_copy_segments): blocks = [(tensor at
+    the block's first plane, its plane stride, column offset in buf, count)].
+    The segment table goes to the device through pinned memory on the
+    current stream."""
+    if not blocks:
+        return
+    table = np.zeros(len(blocks), _SEGMENT)
+    for i, (t, stride, offset, count) in enumerate(blocks):
+        table[i] = (t.data_ptr(), stride, offset, count, 0)
+    dev = torch.from_numpy(table.view(np.uint8)).pin_memory().to(buf.device, non_blocking=True)
+    N.check(N.load().dexmpm_copy_segments(N.ptr(dev), len(blocks), planes, N.ptr(buf), buf_stride, mode,
+                                          int(table["count"].max()), N.stream_ptr()), "dexmpm_copy_segments")
 
 
 @dataclass
@@ -293,20 +314,20 @@ class Server:
         self._round_batches.append(b)
         E = b.E
         ev = [self._mark()]
-        for e, r in enumerate(reqs):
-            res = self.resident[r.rid]
-            o = E.p_off[e]
-            b.slot[0][:, o:o + r.env.n].copy_(res.state)
-            t0 = r.step * self.T
-            bo = E.body_off[e]
-            b.poses[:, bo:bo + r.env.nb].copy_(res.poses[t0:t0 + self.T + 1])
+        # every request's state and poses into the engine: one launch each
+        res_ = [self.resident[r.rid] for r in reqs]
+        np_, nb8 = E.n_particles, b.poses.shape[1] * 8
+        copy_segments([(res.state, r.env.n, E.p_off[e], r.env.n) for e, (r, res) in enumerate(zip(reqs, res_))],
+                      N.STATE_PLANES, b.slot[0], np_, N.SEGMENTS_GATHER)
+        copy_segments([(res.poses[r.step * self.T], r.env.nb * 8, E.body_off[e] * 8, r.env.nb * 8)
+                       for e, (r, res) in enumerate(zip(reqs, res_)) if r.env.nb],
+                      self.T + 1, b.poses, nb8, N.SEGMENTS_GATHER)
         ev.append(self._mark())
         self._run_batch(b, "fwd")
         ev.append(self._mark())
-        for e, r in enumerate(reqs):
-            res = self.resident[r.rid]
-            o = E.p_off[e]
-            res.state.copy_(b.out[:, o:o + r.env.n])
+        copy_segments([(res.state, r.env.n, E.p_off[e], r.env.n) for e, (r, res) in enumerate(zip(reqs, res_))],
+                      N.STATE_PLANES, b.out, np_, N.SEGMENTS_SCATTER)
+        for r, res in zip(reqs, res_):
             if r.grad:
                 res.ckpt.append(res.state.clone())
             self.work += r.env.n * self.T
@@ -319,30 +340,30 @@ class Server:
         E = b.E
         ev = [self._mark()]
         b.gbuf[1].zero_()
-        for e, r in enumerate(reqs):
-            res = self.resident[r.rid]
-            o = E.p_off[e]
-            k = r.horizon - 1 - r.step  # env step being differentiated
-            b.slot[0][:, o:o + r.env.n].copy_(res.ckpt[k])
-            t0 = k * self.T
-            bo = E.body_off[e]
-            b.poses[:, bo:bo + r.env.nb].copy_(res.poses[t0:t0 + self.T + 1])
+        res_ = [self.resident[r.rid] for r in reqs]
+        ks = [r.horizon - 1 - r.step for r in reqs]  # the env step being differentiated
+        for r, res in zip(reqs, res_):
             if res.grad is None:  # loss gradient of the final state: d/dx of mean |x|^2
                 res.grad = torch.zeros_like(res.state)
                 res.grad[0:3] = 2.0 * res.ckpt[-1][0:3] / r.env.n
-            b.gbuf[1][:, o:o + r.env.n].copy_(res.grad)
+        np_, nb8 = E.n_particles, b.poses.shape[1] * 8
+        rows = list(enumerate(zip(reqs, res_, ks)))
+        copy_segments([(res.ckpt[k], r.env.n, E.p_off[e], r.env.n) for e, (r, res, k) in rows],
+                      N.STATE_PLANES, b.slot[0], np_, N.SEGMENTS_GATHER)
+        copy_segments([(res.grad, r.env.n, E.p_off[e], r.env.n) for e, (r, res, k) in rows],
+                      N.STATE_PLANES, b.gbuf[1], np_, N.SEGMENTS_GATHER)
+        copy_segments([(res.poses[k * self.T], r.env.nb * 8, E.body_off[e] * 8, r.env.nb * 8)
+                       for e, (r, res, k) in rows if r.env.nb], self.T + 1, b.poses, nb8, N.SEGMENTS_GATHER)
         b.bgrad.zero_()
         ev.append(self._mark())
         self._run_batch(b, "bwd")
         ev.append(self._mark())
-        for e, r in enumerate(reqs):
-            res = self.resident[r.rid]
-            o = E.p_off[e]
-            k = r.horizon - 1 - r.step
-            res.grad.copy_(b.gbuf[1][:, o:o + r.env.n])
-            bo = E.body_off[e]
-            t0 = k * self.T
-            res.bgrad[t0:t0 + self.T + 1] += b.bgrad[:, bo:bo + r.env.nb]
+        copy_segments([(res.grad, r.env.n, E.p_off[e], r.env.n) for e, (r, res, k) in rows],
+                      N.STATE_PLANES, b.gbuf[1], np_, N.SEGMENTS_SCATTER)
+        copy_segments([(res.bgrad[k * self.T], r.env.nb * 8, E.body_off[e] * 8, r.env.nb * 8)
+                       for e, (r, res, k) in rows if r.env.nb], self.T + 1, b.bgrad, nb8,
+                      N.SEGMENTS_SCATTER_ADD)
+        for r in reqs:
             self.work += r.env.n * self.T
         ev.append(self._mark())
         self._events.append(("bwd", ev))

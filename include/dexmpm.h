@@ -352,6 +352,28 @@ int dexmpm_sort(const DexBatch *b, const DexSortWork *w, const float *s, float *
 int dexmpm_permute(const int32_t *perm, const void *src, void *dst, int n, int planes, int inverse,
                    dexmpm_stream_t stream);
 
+/* One block of a segmented plane copy: `count` consecutive floats in each
+ * of `planes` planes, at `other` (plane q at other + q * other_stride) and
+ * at column `offset` of the shared buffer (plane q at buf + q * buf_stride +
+ * offset). */
+typedef struct {
+  float *other;
+  int32_t other_stride, offset, count, pad;
+} DexSegment; /* 24 bytes */
+
+#define DEXMPM_SEGMENTS_GATHER 0      /* buf <- other */
+#define DEXMPM_SEGMENTS_SCATTER 1     /* other <- buf */
+#define DEXMPM_SEGMENTS_SCATTER_ADD 2 /* other += buf */
+
+/* Many blocks of planes between their own buffers and one shared buffer in
+ * one launch (the serving loop gathers its requests' states, gradients and
+ * poses into an engine and scatters the results back this way).  seg is a
+ * device array of n segments; every segment copies `planes` planes.  The
+ * segments' columns in buf must not overlap for a gather, nor their `other`
+ * blocks for a scatter. */
+int dexmpm_copy_segments(const DexSegment *seg, int n, int planes, float *buf, int buf_stride, int mode,
+                         int max_count, dexmpm_stream_t stream);
+
 /* Copy out and clear the device error word (host pointer out). */
 int dexmpm_get_error(const DexBatch *b, int32_t *out, dexmpm_stream_t stream);
 

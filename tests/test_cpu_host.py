@@ -36,13 +36,15 @@ def test_struct_layouts_match_header():
                 'printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(DexEnv), offsetof(DexEnv, gravity), '
                 'sizeof(DexBatch), offsetof(DexBatch, grid), offsetof(DexBatch, block_count), '
                 'offsetof(DexBatch, error), sizeof(DexSortWork), offsetof(DexSortWork, partial)); '
-                'printf("%zu\\n", offsetof(DexBatch, block_xyz)); return 0;}\n')
+                'printf("%zu %zu %zu\\n", offsetof(DexBatch, block_xyz), sizeof(DexSegment), '
+                'offsetof(DexSegment, count)); return 0;}\n')
     exe = src[:-2]
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
     got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(N.DexEnv), N.DexEnv.gravity.offset, ctypes.sizeof(N.DexBatch), N.DexBatch.grid.offset,
             N.DexBatch.block_count.offset, N.DexBatch.error.offset, ctypes.sizeof(N.DexSortWork),
-            N.DexSortWork.partial.offset, N.DexBatch.block_xyz.offset]
+            N.DexSortWork.partial.offset, N.DexBatch.block_xyz.offset, ctypes.sizeof(N.DexSegment),
+            N.DexSegment.count.offset]
     assert got == want
 
 
@@ -364,6 +366,21 @@ def test_fused_adjoint_entry_checks_arguments(native_lib):
     b.vout_grad = 1
     b.n_tiles = 0
     assert f(bp, 3, 2, one, two, three, four, three, None, None) == 0                     # g_prev may be g_next
+
+
+def test_copy_segments_checks_arguments(native_lib):
+    """dexmpm_copy_segments rejects bad counts and modes before any CUDA
+    call, and returns OK without a launch when there is nothing to copy."""
+    import ctypes
+    f = native_lib.dexmpm_copy_segments
+    one = ctypes.c_void_p(1)
+    ARG = 1
+    assert f(one, -1, 24, one, 100, 0, 10, None) == ARG          # negative segment count
+    assert f(one, 2, 24, one, 100, 3, 10, None) == ARG           # unknown mode
+    assert f(one, 70000, 24, one, 100, 0, 10, None) == ARG       # more segments than one launch holds
+    assert f(None, 2, 24, one, 100, 0, 10, None) == ARG          # no table
+    assert f(None, 0, 24, None, 100, 0, 10, None) == 0           # nothing to copy
+    assert f(one, 2, 24, one, 100, 1, 0, None) == 0              # empty segments
 
 
 def test_render_launchers_reject_bad_arguments(native_lib):

@@ -134,6 +134,36 @@ def test_serving_relays_out_instead_of_rebuilding(cuda):
     assert br["relayouts"] == srv.relayouts
 
 
+def test_copy_segments_gathers_scatters_and_adds(cuda):
+    """dexmpm_copy_segments: blocks of planes of different lengths and
+    strides into columns of one buffer and back (copy and add), exactly."""
+    from dexdeform_gb300 import _native as N
+    from dexdeform_gb300.serving import copy_segments
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    planes, stride = 5, 1000
+    parts = [torch.randn((planes, n), device="cuda", generator=gen) for n in (7, 300, 1, 129)]
+    offs = [0, 10, 400, 600]
+    buf = torch.zeros((planes, stride), device="cuda")
+    copy_segments([(t, t.shape[1], o, t.shape[1]) for t, o in zip(parts, offs)], planes, buf, stride,
+                  N.SEGMENTS_GATHER)
+    for t, o in zip(parts, offs):
+        assert torch.equal(buf[:, o:o + t.shape[1]], t)
+    assert float(buf[:, 310:400].abs().sum()) == 0.0
+    buf.mul_(2.0)
+    back = [torch.zeros_like(t) for t in parts]
+    copy_segments([(t, t.shape[1], o, t.shape[1]) for t, o in zip(back, offs)], planes, buf, stride,
+                  N.SEGMENTS_SCATTER)
+    copy_segments([(t, t.shape[1], o, t.shape[1]) for t, o in zip(parts, offs)], planes, buf, stride,
+                  N.SEGMENTS_SCATTER_ADD)
+    for t, b, o in zip(parts, back, offs):
+        assert torch.equal(b, buf[:, o:o + t.shape[1]]) and torch.allclose(t, 1.5 * b)
+    # a block that is a row range of a larger tensor (the poses of some substeps)
+    poses = torch.randn((30, 3, 8), device="cuda", generator=gen)
+    pbuf = torch.zeros((11, 5, 8), device="cuda")
+    copy_segments([(poses[12], 3 * 8, 2 * 8, 3 * 8)], 11, pbuf, 5 * 8, N.SEGMENTS_GATHER)
+    assert torch.equal(pbuf[:, 2:5], poses[12:23])
+
+
 def test_admission_respects_budget(cuda):
     from dexdeform_gb300.serving import Server
     T = 10
