@@ -280,7 +280,7 @@ class GradModel:
 
         if not (self.use_graphs and torch.is_grad_enabled() and (q.requires_grad or action.requires_grad)):
             return fk(q, action)  # no gradient wanted: plain forward
-        key = (s, q.requires_grad, action.requires_grad)
+        key = (s, q.requires_grad, action.requires_grad, tuple(q.shape), tuple(action.shape), q.dtype, action.dtype)
         g = self._fk_graphs.get(key)
         if g is None:
             sample = (q.detach().clone().requires_grad_(q.requires_grad),
