@@ -369,22 +369,27 @@ __global__ void __launch_bounds__(256) k_permute(const int32_t *__restrict__ per
   }
 }
 
-// Segmented plane copy: blockIdx.y = segment, x-threads over its columns,
-// each thread all planes of its column.
-__global__ void __launch_bounds__(256) k_copy_segments(const DexSegment *__restrict__ seg, int planes,
+// Segmented plane copy: blockIdx.y = segment, x-threads over its (plane,
+// column) elements, one independent load and store each.  The segment table
+// travels in the launch parameters (12 KB of the 32 KB they may hold).
+struct SegmentTable {
+  DexSegment s[DEXMPM_SEGMENTS_PER_LAUNCH];
+};
+__global__ void __launch_bounds__(256) k_copy_segments(const __grid_constant__ SegmentTable tab, int planes,
                                                        float *__restrict__ buf, int buf_stride, int mode) {
-  const DexSegment s = seg[blockIdx.y];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.count; i += gridDim.x * blockDim.x) {
-    for (int q = 0; q < planes; ++q) {
-      float *o = s.other + (size_t)q * s.other_stride + i;
-      float *b = buf + (size_t)q * buf_stride + s.offset + i;
-      if (mode == DEXMPM_SEGMENTS_GATHER)
-        *b = *o;
-      else if (mode == DEXMPM_SEGMENTS_SCATTER)
-        *o = *b;
-      else
-        *o += *b;
-    }
+  const DexSegment s = tab.s[blockIdx.y];
+  const long long total = (long long)planes * s.count;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(e / s.count), i = (int)(e - (long long)q * s.count);
+    float *o = s.other + (size_t)q * s.other_stride + i;
+    float *b = buf + (size_t)q * buf_stride + s.offset + i;
+    if (mode == DEXMPM_SEGMENTS_GATHER)
+      *b = *o;
+    else if (mode == DEXMPM_SEGMENTS_SCATTER)
+      *o = *b;
+    else
+      *o += *b;
   }
 }
 
@@ -442,15 +447,22 @@ int dexmpm_sort(const DexBatch *b, const DexSortWork *w, const float *s, float *
 
 int dexmpm_copy_segments(const DexSegment *seg, int n, int planes, float *buf, int buf_stride, int mode,
                          int max_count, dexmpm_stream_t stream) {
-  if (n < 0 || planes < 0 || max_count < 0 || buf_stride < 0 || n > 65535 || mode < DEXMPM_SEGMENTS_GATHER ||
+  if (n < 0 || planes < 0 || max_count < 0 || buf_stride < 0 || mode < DEXMPM_SEGMENTS_GATHER ||
       mode > DEXMPM_SEGMENTS_SCATTER_ADD)
     return DEXMPM_ERR_ARG;
   if (n == 0 || planes == 0 || max_count == 0) return DEXMPM_OK;
   if (!seg || !buf) return DEXMPM_ERR_ARG;
-  const int per_seg = (max_count + 255) / 256;
-  const dim3 grid(per_seg < 64 ? per_seg : 64, n);
-  k_copy_segments<<<grid, 256, 0, (cudaStream_t)stream>>>(seg, planes, buf, buf_stride, mode);
-  return check_launch();
+  const long long elems = (long long)planes * max_count;
+  const int per_seg = (int)((elems + 255) / 256 < 512 ? (elems + 255) / 256 : 512);
+  for (int first = 0; first < n; first += DEXMPM_SEGMENTS_PER_LAUNCH) {
+    const int m = n - first < DEXMPM_SEGMENTS_PER_LAUNCH ? n - first : DEXMPM_SEGMENTS_PER_LAUNCH;
+    SegmentTable tab;
+    for (int i = 0; i < m; ++i) tab.s[i] = seg[first + i];
+    const dim3 grid(per_seg, m);
+    k_copy_segments<<<grid, 256, 0, (cudaStream_t)stream>>>(tab, planes, buf, buf_stride, mode);
+    if (int rc = check_launch()) return rc;
+  }
+  return DEXMPM_OK;
 }
 
 int dexmpm_permute(const int32_t *perm, const void *src, void *dst, int n, int planes, int inverse,

@@ -27,6 +27,7 @@ substeps in the same order alone or in the mix.
 from __future__ import annotations
 
 import collections
+import ctypes
 import math
 import time
 from dataclasses import dataclass, field
@@ -47,16 +48,16 @@ def copy_segments(blocks, planes: int, buf: torch.Tensor, buf_stride: int, mode:
     """Copy many blocks of `planes` planes between their own tensors and one
     shared buffer in one launch (dexmpm_copy_segments): blocks = [(tensor at
     the block's first plane, its plane stride, column offset in buf, count)].
-    The segment table goes to the device through pinned memory on the
-    current stream."""
+    The segment table is a host array the library passes in the launch
+    parameters."""
     if not blocks:
         return
     table = np.zeros(len(blocks), _SEGMENT)
     for i, (t, stride, offset, count) in enumerate(blocks):
         table[i] = (t.data_ptr(), stride, offset, count, 0)
-    dev = torch.from_numpy(table.view(np.uint8)).pin_memory().to(buf.device, non_blocking=True)
-    N.check(N.load().dexmpm_copy_segments(N.ptr(dev), len(blocks), planes, N.ptr(buf), buf_stride, mode,
-                                          int(table["count"].max()), N.stream_ptr()), "dexmpm_copy_segments")
+    N.check(N.load().dexmpm_copy_segments(table.ctypes.data_as(ctypes.c_void_p), len(blocks), planes, N.ptr(buf),
+                                          buf_stride, mode, int(table["count"].max()), N.stream_ptr()),
+            "dexmpm_copy_segments")
 
 
 @dataclass

@@ -366,11 +366,14 @@ typedef struct {
 #define DEXMPM_SEGMENTS_SCATTER_ADD 2 /* other += buf */
 
 /* Many blocks of planes between their own buffers and one shared buffer in
- * one launch (the serving loop gathers its requests' states, gradients and
- * poses into an engine and scatters the results back this way).  seg is a
- * device array of n segments; every segment copies `planes` planes.  The
- * segments' columns in buf must not overlap for a gather, nor their `other`
- * blocks for a scatter. */
+ * one launch per DEXMPM_SEGMENTS_PER_LAUNCH segments (the serving loop
+ * gathers its requests' states, gradients and poses into an engine and
+ * scatters the results back this way).  seg is a HOST array of n segments,
+ * passed to the kernel in its launch parameters (no copy to the device and
+ * no synchronisation; the array may be reused as soon as the call returns);
+ * every segment copies `planes` planes.  The segments' columns in buf must
+ * not overlap for a gather, nor their `other` blocks for a scatter. */
+#define DEXMPM_SEGMENTS_PER_LAUNCH 512
 int dexmpm_copy_segments(const DexSegment *seg, int n, int planes, float *buf, int buf_stride, int mode,
                          int max_count, dexmpm_stream_t stream);
 

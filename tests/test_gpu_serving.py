@@ -157,6 +157,11 @@ def test_copy_segments_gathers_scatters_and_adds(cuda):
                   N.SEGMENTS_SCATTER_ADD)
     for t, b, o in zip(parts, back, offs):
         assert torch.equal(b, buf[:, o:o + t.shape[1]]) and torch.allclose(t, 1.5 * b)
+    # more segments than one launch carries (512 per launch)
+    many = [torch.randn((planes, 3), device="cuda", generator=gen) for _ in range(600)]
+    wide = torch.zeros((planes, 3 * 600), device="cuda")
+    copy_segments([(t, 3, 3 * i, 3) for i, t in enumerate(many)], planes, wide, 3 * 600, N.SEGMENTS_GATHER)
+    assert torch.equal(wide, torch.cat(many, 1))
     # a block that is a row range of a larger tensor (the poses of some substeps)
     poses = torch.randn((30, 3, 8), device="cuda", generator=gen)
     pbuf = torch.zeros((11, 5, 8), device="cuda")
