@@ -16,6 +16,7 @@ Layouts (see include/dexmpm.h): state slot = 24 planes x n_particles
 from __future__ import annotations
 
 import ctypes
+import gc
 import math
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
@@ -910,10 +911,19 @@ def run_graph(E: BatchEngine, cache: dict, key, fn, use_graphs: bool = True):
         g = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side):
-            g.capture_begin()
-            fn()
-            g.capture_end()
+        # no garbage collection during the capture: a finalizer that calls
+        # CUDA (an event or graph of an object going out of scope) would
+        # invalidate it
+        enabled = gc.isenabled()
+        gc.disable()
+        try:
+            with torch.cuda.stream(side):
+                g.capture_begin()
+                fn()
+                g.capture_end()
+        finally:
+            if enabled:
+                gc.enable()
         torch.cuda.current_stream().wait_stream(side)
         E.fslot, E.launches = f1, l0 + dl
         cache[(key, f1)] = (g, df, dl)

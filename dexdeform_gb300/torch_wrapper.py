@@ -16,6 +16,7 @@ forward kinematics of joint-velocity controls -- is differentiated through.
 from __future__ import annotations
 
 import ctypes
+import gc
 from typing import Optional, Sequence
 
 import numpy as np
@@ -285,7 +286,16 @@ class GradModel:
         if g is None:
             sample = (q.detach().clone().requires_grad_(q.requires_grad),
                       action.detach().clone().requires_grad_(action.requires_grad))
-            g = self._fk_graphs[key] = torch.cuda.make_graphed_callables(fk, sample)
+            # no garbage collection while the graphs are captured: a finalizer
+            # that calls CUDA (an event, stream or graph of an object going
+            # out of scope) would invalidate the capture
+            enabled = gc.isenabled()
+            gc.disable()
+            try:
+                g = self._fk_graphs[key] = torch.cuda.make_graphed_callables(fk, sample)
+            finally:
+                if enabled:
+                    gc.enable()
         return g(q, action)
 
     def forward(self, s, action, *past_obs):

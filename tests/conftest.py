@@ -43,6 +43,19 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
+def within_spread(got, want, again, bars, factor=4.0):
+    """Schedule-equivalence check: every pair (got[i], want[i]) within
+    max(bars[i], factor x rel(again[i], want[i])), where `again` repeats the
+    run that gave `want` (the spread of two identical runs: float atomics add
+    in a different order each time)."""
+    for i, (a, b, c, bar) in enumerate(zip(got, want, again, bars)):
+        if b is None:
+            continue
+        n = rel(c, b)
+        err = rel(a, b)
+        assert err < max(bar, factor * n), (i, err, bar, n)
+
+
 def golden_env(path):
     """Rebuild the workloads.Env a fixture was generated from."""
     from dexdeform_gb300 import workloads as W

@@ -420,3 +420,15 @@ def test_sort_entry_points_check_arguments(native_lib):
     assert perm(None, one, two, 32, 24, 0, None) == N.ERR_ARG                       # no permutation
     assert perm(one, one, two, -1, 24, 0, None) == N.ERR_ARG                        # negative size
     assert perm(one, one, two, 0, 24, 0, None) == N.OK                              # nothing to move
+
+
+def test_product_modules_import():
+    """Every module of the package imports on a machine without a GPU (no
+    CUDA call at import time)."""
+    import importlib
+    import pkgutil
+    import dexdeform_gb300
+    names = [m.name for m in pkgutil.iter_modules(dexdeform_gb300.__path__)]
+    assert {"engine", "serving", "simulator", "torch_wrapper", "shadow_hand", "hand"} <= set(names)
+    for name in names:
+        importlib.import_module(f"dexdeform_gb300.{name}")
