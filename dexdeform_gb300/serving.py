@@ -7,12 +7,17 @@ running requests together one env step (``substeps`` substeps) per round:
 
   * forward-phase requests (rollouts, and gradient requests before their
     horizon) form one batch: the particle states are gathered into a
-    BatchEngine arena, stepped, and scattered back; gradient requests keep a
-    checkpoint per env step;
+    BatchEngine arena (one launch for all requests, dexmpm_copy_segments),
+    ordered by grid cell on the device, stepped, and scattered back in the
+    requests' own order; gradient requests keep a checkpoint per env step;
   * backward-phase requests (gradient requests past their horizon) form a
     second batch that runs one env step of the adjoint (recompute from the
     checkpoint, reverse substeps) per round, on its own CUDA stream so that
     it overlaps the forward batch on the device.
+
+Requests may hand over their particles in any order (Server(sort=True)
+re-orders every round's gathered particles by grid cell, with their material
+and incoming gradients, and maps the results back).
 
 Membership changes at round boundaries (a request that arrives while others
 run joins at the next round; a finished request leaves and frees its memory).
