@@ -68,7 +68,13 @@ using namespace dexmpm;
 #ifndef DEX_DIRECT_SEGS
 #define DEX_DIRECT_SEGS 8
 #endif
+// Scatter: unrolling of the walk over a segment's positions (the sum keeps
+// its order, so the unrolling changes no result).
+#ifndef DEX_WALK_UNROLL
+#define DEX_WALK_UNROLL 4
+#endif
 constexpr int kG2pGradUnroll = DEX_G2P_GRAD_UNROLL;
+constexpr int kWalkUnroll = DEX_WALK_UNROLL;
 
 namespace {
 
@@ -376,6 +382,7 @@ __device__ __forceinline__ void red_walk(const float *red, const Ranked &R, int 
     rest &= rest - 1u;
     const int end = rest ? __ffs(rest) - 1 : R.n_live;
     float2 acc = make_float2(0.f, 0.f);
+#pragma unroll kWalkUnroll
     for (int q = start; q < end; ++q) {
       const float2 t = *reinterpret_cast<const float2 *>(col + 4 * q);
       acc.x += t.x;
