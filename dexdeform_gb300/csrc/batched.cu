@@ -66,7 +66,7 @@ using namespace dexmpm;
 // Scatter: warps with more than DEX_DIRECT_SEGS segments of equal stencil
 // base use per-lane atomics instead of the transposed reduction.
 #ifndef DEX_DIRECT_SEGS
-#define DEX_DIRECT_SEGS 8
+#define DEX_DIRECT_SEGS 12
 #endif
 // Scatter: unrolling of the walk over a segment's positions (the sum keeps
 // its order, so the unrolling changes no result).
@@ -279,8 +279,13 @@ __device__ __forceinline__ void red_add4(float *dst, float a, float b, float c, 
 constexpr int kRedRow = 132;  // floats per node row (32 lanes x 4 + 4 pad)
 constexpr int kDirectSegs = DEX_DIRECT_SEGS;
 constexpr int kSegTable = 16 * kRedRow;                      // after the 16 node rows
-constexpr int kRedWarpFloats = kSegTable + 9 * kDirectSegs;  // + 9 cell terms per segment
+// + 9 cell terms per segment, rounded up to 4 floats: every warp's buffer
+// must start on a 16-byte boundary for the float4 row stores and float2
+// row loads (a stride of 2,166 floats, with 6 segments, misaligns odd warps)
+constexpr int kRedWarpFloats = (kSegTable + 9 * kDirectSegs + 3) & ~3;
 constexpr size_t kScatterSmemPerWarp = sizeof(float) * kRedWarpFloats;
+static_assert(kRedWarpFloats % 4 == 0, "per-warp scatter buffers must stay 16-byte aligned");
+static_assert(kDirectSegs >= 1 && kDirectSegs <= 32, "a warp has 1 to 32 segments");
 
 __device__ __forceinline__ float *warp_red_buffer() {
   extern __shared__ float4 s_dyn[];
@@ -1301,12 +1306,17 @@ __global__ void k_reset_counts(DexBatch B) {
 
 int check_launch() { return cudaGetLastError() == cudaSuccess ? DEXMPM_OK : DEXMPM_ERR_LAUNCH; }
 
+// The kernels read and write the grid slots, their velocities and adjoints,
+// the body shapes and the poses as float4: those must start on 16-byte
+// boundaries (an offset pointer would fault the kernel, so it is refused).
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 bool valid(const DexBatch *b) {
   return b && b->envs && b->tiles && b->block_env && b->block_xyz && b->mass && b->vol && b->mu_lam_yield && b->grid &&
          b->vout &&
          b->block_flag && b->block_list && b->block_count && b->done_counter && b->error && b->n_tiles >= 0 &&
          b->n_blocks > 0 && b->n_slots > 0 && (b->tile_size == 64 || b->tile_size == 128 || b->tile_size == 256) &&
-         b->grid_ctas > 0;
+         b->grid_ctas > 0 && aligned16(b->grid) && aligned16(b->vout) && aligned16(b->body_shape);
 }
 bool slot_ok(const DexBatch *b, int k) { return k >= 0 && k < b->n_slots; }
 
@@ -1351,7 +1361,9 @@ int scatter_attr_ready() {
   ready[dev].store(1, std::memory_order_release);
   return DEXMPM_OK;
 }
-bool grad_ok(const DexBatch *b) { return valid(b) && b->vout_grad && b->in_grad; }
+bool grad_ok(const DexBatch *b) {
+  return valid(b) && b->vout_grad && b->in_grad && aligned16(b->vout_grad) && aligned16(b->in_grad);
+}
 
 // Kernel launch on the caller's stream; returns the launch status.
 template <typename... P, typename... A>
@@ -1392,7 +1404,8 @@ int dexmpm_grid_op(const DexBatch *b, int slot, int clear_slot, const float *pos
                    dexmpm_stream_t stream) {
   if (!valid(b) || !slot_ok(b, slot) || (clear_slot >= 0 && (!slot_ok(b, clear_slot) || clear_slot == slot)))
     return DEXMPM_ERR_ARG;
-  if (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape)) return DEXMPM_ERR_ARG;
+  if (b->n_bodies > 0 && (!pose || !next_pose || !b->body_shape || !aligned16(pose) || !aligned16(next_pose)))
+    return DEXMPM_ERR_ARG;
   return launch(k_grid_op, grid_ctas(b, (const void *)k_grid_op, kGridOp), 256, 0, stream, *b, slot,
                 clear_slot < 0 ? -1 : clear_slot, pose, next_pose);
 }
@@ -1435,7 +1448,9 @@ int dexmpm_g2p_grad(const DexBatch *b, int slot, const float *S, const float *Sn
 int dexmpm_grid_op_grad(const DexBatch *b, int slot, const float *pose, const float *next_pose, float *bgrad,
                         float *next_bgrad, dexmpm_stream_t stream) {
   if (!grad_ok(b) || !slot_ok(b, slot)) return DEXMPM_ERR_ARG;
-  if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape)) return DEXMPM_ERR_ARG;
+  if (b->n_bodies > 0 && (!pose || !next_pose || !bgrad || !next_bgrad || !b->body_shape || !aligned16(pose) ||
+                          !aligned16(next_pose)))
+    return DEXMPM_ERR_ARG;
   return launch(k_grid_op_grad, grid_ctas(b, (const void *)k_grid_op_grad, kGridOpGrad), 256, 0, stream, *b, slot,
                 pose, next_pose, bgrad, next_bgrad);
 }

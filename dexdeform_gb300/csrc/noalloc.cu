@@ -115,7 +115,10 @@ extern "C" int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *
   if (e.gx < 8 || e.gy < 8 || e.gz < 8 || (e.gx & 3) || (e.gy & 3) || (e.gz & 3)) return DEXMPM_ERR_ARG;
   if ((long long)e.gx * e.gy * e.gz > kMaxCells) return DEXMPM_ERR_ARG;
   if (e.n_bodies < 0 || e.n_bodies > DEXMPM_MAX_BODIES) return DEXMPM_ERR_ARG;
-  if (e.n_bodies > 0 && (!body_shape || !pose || !next_pose)) return DEXMPM_ERR_ARG;
+  // body shapes and poses are read as float4: 16-byte boundaries
+  auto a16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  if (e.n_bodies > 0 && (!body_shape || !pose || !next_pose || !a16(body_shape) || !a16(pose) || !a16(next_pose)))
+    return DEXMPM_ERR_ARG;
   void *addr = nullptr;
   int rc = scratch_address(&addr);
   if (rc) return rc;

@@ -403,9 +403,11 @@ int device_sms() {
   return sms;
 }
 
+// cell_count and cell_start are read and written as int2, block_total as int4
 bool work_ok(const DexSortWork *w) {
   return w && w->cell_count && w->cell_start && w->block_total && w->block_base && w->block_flag && w->block_list &&
-         w->rank && w->key && w->partial && w->counters;
+         w->rank && w->key && w->partial && w->counters && (reinterpret_cast<uintptr_t>(w->cell_count) & 7u) == 0 &&
+         (reinterpret_cast<uintptr_t>(w->cell_start) & 7u) == 0 && (reinterpret_cast<uintptr_t>(w->block_total) & 15u) == 0;
 }
 
 bool batch_ok(const DexBatch *b) {

@@ -349,7 +349,7 @@ def test_fused_adjoint_entry_checks_arguments(native_lib):
     for f, _ in N.DexBatch._fields_:
         if f not in ("n_envs", "n_particles", "n_tiles", "n_blocks", "n_bodies", "tile_size", "grid_ctas", "flags",
                      "n_slots", "pad0", "pad1", "pad2"):
-            setattr(b, f, 1)
+            setattr(b, f, 4096)  # 16-byte aligned, as the float4 buffers must be
     b.n_envs, b.n_particles, b.n_tiles, b.n_blocks, b.n_bodies = 1, 32, 1, 8, 0
     b.tile_size, b.grid_ctas, b.n_slots = 128, 8, 6
     f = native_lib.dexmpm_p2g_g2p_grad
@@ -363,7 +363,7 @@ def test_fused_adjoint_entry_checks_arguments(native_lib):
     assert f(bp, 3, 2, None, two, three, four, one, None, None) == ARG                    # no state
     b.vout_grad = None
     assert f(bp, 3, 2, one, two, three, four, one, None, None) == ARG                     # no gradient grids
-    b.vout_grad = 1
+    b.vout_grad = 4096
     b.n_tiles = 0
     assert f(bp, 3, 2, one, two, three, four, three, None, None) == 0                     # g_prev may be g_next
 
@@ -409,17 +409,64 @@ def test_sort_entry_points_check_arguments(native_lib):
     b.envs, b.tiles = 1, 1
     w = N.DexSortWork()
     for f, _ in N.DexSortWork._fields_:
-        setattr(w, f, 1)
+        setattr(w, f, 4096)  # never dereferenced: every call below is refused first
     sort, perm = native_lib.dexmpm_sort, native_lib.dexmpm_permute
     assert sort(None, ctypes.byref(w), one, two, one, None) == N.ERR_ARG          # no batch
     assert sort(ctypes.byref(b), None, one, two, one, None) == N.ERR_ARG          # no scratch
     assert sort(ctypes.byref(b), ctypes.byref(w), one, one, one, None) == N.ERR_ARG  # in place
     w.rank = None
     assert sort(ctypes.byref(b), ctypes.byref(w), one, two, one, None) == N.ERR_ARG  # incomplete scratch
+    w.rank = 4096
+    w.cell_count = 4100
+    assert sort(ctypes.byref(b), ctypes.byref(w), one, two, one, None) == N.ERR_ARG  # cell counts read as int2
+    w.cell_count, w.block_total = 4096, 4104
+    assert sort(ctypes.byref(b), ctypes.byref(w), one, two, one, None) == N.ERR_ARG  # block totals read as int4
     assert perm(one, one, one, 32, 24, 0, None) == N.ERR_ARG                        # in place
     assert perm(None, one, two, 32, 24, 0, None) == N.ERR_ARG                       # no permutation
     assert perm(one, one, two, -1, 24, 0, None) == N.ERR_ARG                        # negative size
     assert perm(one, one, two, 0, 24, 0, None) == N.OK                              # nothing to move
+
+
+def test_batch_launchers_refuse_unaligned_vector_buffers(native_lib):
+    """The kernels read and write the grid slots, their velocities and
+    adjoints, the body shapes and the poses as float4: a buffer that does not
+    start on a 16-byte boundary is refused with DEXMPM_ERR_ARG before any CUDA
+    call (with no particle tiles an accepted call returns OK unlaunched)."""
+    import ctypes
+    from dexdeform_gb300 import _native as N
+    b = N.DexBatch()
+    b.n_envs, b.n_particles, b.n_tiles, b.n_blocks, b.n_bodies = 1, 32, 0, 8, 1
+    b.tile_size, b.grid_ctas, b.n_slots = 128, 1, 2
+    for f, t in N.DexBatch._fields_:
+        if t is ctypes.c_void_p:
+            setattr(b, f, 4096)  # never dereferenced
+    s, t = ctypes.c_void_p(8192), ctypes.c_void_p(12288)
+    g2p, g2p_grad = native_lib.dexmpm_g2p, native_lib.dexmpm_g2p_grad
+    assert g2p(ctypes.byref(b), 0, s, t, None) == N.OK
+    assert g2p_grad(ctypes.byref(b), 0, s, t, s, t, None) == N.OK
+    for field in ("grid", "vout", "body_shape"):
+        setattr(b, field, 4104)
+        assert g2p(ctypes.byref(b), 0, s, t, None) == N.ERR_ARG, field
+        setattr(b, field, 4096)
+    for field in ("vout_grad", "in_grad"):
+        setattr(b, field, 4104)
+        assert g2p_grad(ctypes.byref(b), 0, s, t, s, t, None) == N.ERR_ARG, field
+        assert g2p(ctypes.byref(b), 0, s, t, None) == N.OK  # the forward does not use it
+        setattr(b, field, 4096)
+    odd = ctypes.c_void_p(8200)
+    assert native_lib.dexmpm_grid_op(ctypes.byref(b), 0, -1, odd, s, None) == N.ERR_ARG
+    assert native_lib.dexmpm_grid_op(ctypes.byref(b), 0, -1, s, odd, None) == N.ERR_ARG
+    assert native_lib.dexmpm_grid_op_grad(ctypes.byref(b), 0, odd, s, s, t, None) == N.ERR_ARG
+    assert native_lib.dexmpm_grid_op_grad(ctypes.byref(b), 0, s, odd, s, t, None) == N.ERR_ARG
+    # the allocation-free entry point, on an otherwise valid 8^3 env with one body
+    e = N.DexEnv()
+    e.n, e.gx, e.gy, e.gz, e.n_bodies = 32, 8, 8, 8, 1
+    e.dx, e.inv_dx, e.dt = 0.125, 8.0, 1e-4
+    one = ctypes.c_void_p(4096)
+    f = native_lib.dexmpm_substep_noalloc
+    assert f(ctypes.byref(e), one, s, one, one, one, odd, one, one, one, None) == N.ERR_ARG  # body shapes
+    assert f(ctypes.byref(e), one, s, one, one, one, one, odd, one, one, None) == N.ERR_ARG  # pose
+    assert f(ctypes.byref(e), one, s, one, one, one, one, one, odd, one, None) == N.ERR_ARG  # next pose
 
 
 def test_product_modules_import():
