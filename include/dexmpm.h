@@ -173,6 +173,11 @@ int render(float *sdf_volume, float *box_min, float *box_max, float *color_volum
  * Gradient grids (one each): vout_grad dL/dv_out, in_grad (dL/d(mv), dL/dm);
  *   the grid adjoint zeroes vout_grad after reading it and writes in_grad for
  *   every cell of its blocks.
+ * Alignment: the kernels read and write grid, vout, vout_grad, in_grad,
+ *   body_shape and the pose arrays as float4, so each must start on a 16-byte
+ *   boundary (cudaMalloc'd buffers and whole rows of them do); the launchers
+ *   return DEXMPM_ERR_ARG for one that does not.  State, material, tape and
+ *   pose-gradient arrays need only float alignment.
  * Poses: [n_bodies][8] floats per substep boundary: p.x p.y p.z 0 q.w q.x q.y q.z.
  * Body shapes: [n_bodies][8]: type friction softness round, args w x y z.
  * Body-pose gradients: [n_bodies][8] in the pose layout, accumulated.
@@ -320,7 +325,9 @@ int dexmpm_substep_noalloc(const DexEnv *env, const float *s, float *next_s, con
  * scatters in the caller's order (mpm/csrc/integrator.cu:312-394).
  *
  * DexSortWork: caller-owned device scratch, all zero before the first sort
- * (each sort leaves cell_count, block_total, block_flag and counters zero). */
+ * (each sort leaves cell_count, block_total, block_flag and counters zero).
+ * cell_count and cell_start are accessed as int2 (8-byte aligned starts),
+ * block_total as int4 (16-byte aligned); otherwise DEXMPM_ERR_ARG. */
 #define DEXMPM_STATE_PLANES 24
 #define DEXMPM_SORT_CHUNK 4096 /* block totals per scan CTA */
 #define DEXMPM_SORT_PARTIALS(n_blocks) (((n_blocks) + DEXMPM_SORT_CHUNK - 1) / DEXMPM_SORT_CHUNK)
