@@ -505,26 +505,27 @@ ALG_BYTES = {
 
 
 # DRAM bytes (read + write) per particle of one launch, from ncu captures
-# on the 64-env batch (profiles/k_*_batch64.md)
-NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 144.833024e6 / 654552,
-                               "g2p2g": 63.928576e6 / 654552, "p2g2g_grad": 234.343168e6 / 654552}
+# on the 64-env batch (profiles/k_*_batch64.md; the fused kernels' from the
+# captures of profiles/l2_atomics_batch64.md)
+NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 142.285376e6 / 654552,
+                               "g2p2g": 63.428544e6 / 654552, "p2g2g_grad": 232.012544e6 / 654552}
 # L2 reduction traffic and the busy fraction of the L2 atomic units of one
 # launch, from an ncu capture on the same batch (profiles/l2_atomics_batch64.md):
 # (lts__t_requests_op_red.sum, lts__t_sectors_op_red.sum,
 #  lts__d_atomic_input_cycles_active.avg.pct_of_peak_sustained_elapsed)
-NCU_L2_RED = {"g2p2g": (3212980, 5181759, 10.93), "g2p2g_tape": (3215606, 5185041, 10.06),
-              "p2g2g_grad": (3208150, 5169492, 7.56)}
+NCU_L2_RED = {"g2p2g": (2156514, 3752499, 8.13), "g2p2g_tape": (2158644, 3754360, 7.76),
+              "p2g2g_grad": (2167977, 3771161, 5.50)}
 
 # what limits each dominant kernel function, from its ncu capture on the same
 # batch (--set full): issue-active and DRAM throughput percentages, warps
 # active, and the reading of the stall counters
 NCU_LIMITER = {
-    "k_g2p2g": {"issue_active_pct": {"tape": 57.4, "forward": 60.9}, "dram_throughput_pct": {"tape": 19.8, "forward": 9.4},
-                "warps_active_pct": 33.3,
+    "k_g2p2g": {"issue_active_pct": {"tape": 60.5, "forward": 60.9}, "dram_throughput_pct": {"tape": 19.9, "forward": 9.4},
+                "warps_active_pct": 33.1,
                 "reading": "instruction issue: G2P gather, SVD, return mapping and the 27-node scatter; "
                            "long-scoreboard the top stall",
                 "source": "profiles/k_g2p2g_batch64.md"},
-    "k_p2g2g_grad": {"issue_active_pct": 49.8, "dram_throughput_pct": 24.9, "warps_active_pct": 28.4,
+    "k_p2g2g_grad": {"issue_active_pct": 50.7, "dram_throughput_pct": 25.1, "warps_active_pct": 28.8,
                      "reading": "latency: streamed planes and dependent stress/SVD adjoint arithmetic at 20 "
                                 "warps per SM",
                      "source": "profiles/k_p2g2g_grad_batch64.md"},
