@@ -293,6 +293,91 @@ def test_config1_full_size_gradients(cuda):
     assert (err < 0.25).sum() >= 10, (fd, an)
 
 
+def test_config1_env_step_adjoints_match_oracle(cuda, oracle_mod):
+    """Config 1 at full size (20,000 particles, 22 capsules of the hand, 20
+    env steps x 50 substeps), each env step's adjoint against the FP64
+    oracle's on the same inputs.
+
+    The rollout's backward is recorded link by link: for an env step, the
+    state it started from (the checkpoint), its 51 body poses, the gradient
+    that reached its output after the later env steps' adjoints, and the
+    gradients it returned (initial state; body poses of every substep
+    boundary).  The oracle recomputes that env step's 50 substeps from the
+    same checkpoint (FP64, the state rounded to FP32 between substeps as the
+    reference stores it) and chains its substep adjoints
+    (mpm/simulator.py:573-585) from the same incoming gradient, with the exact
+    capsule-normal derivative the model uses.  Every one of the 20 links is
+    checked; the deepest, env step 0, sees the gradient after 19 env steps of
+    backpropagation.  Unlike central differences through 1,000 substeps, this
+    needs no smoothness across contact thresholds.
+
+    Bars, relative L2 per field: 4x the largest distance the reference's own
+    FP32 kernels show from this oracle on the full-size batch adjoint
+    (tests/golden/ref_batch_adjoint.npz; 1e-3 at least), i.e. x 8.2e-3,
+    v 7.2e-3, F 1.1e-2, C 7.1e-3, pose position 7.3e-2, pose rotation
+    4.5e-2.  Measured on GB300, the links' largest distances are 6.4e-4,
+    1.3e-4, 2.9e-3, 2.8e-3, 2.3e-2 and 1.8e-2.  Both the FP32 rounding of the
+    pose rows (each a small difference of sums of order 1/dt over every node
+    a body touches) and the reference's own distances are of that size; a
+    missing or wrong adjoint term is off by 10% or more."""
+    import dataclasses
+    import os
+    from conftest import GOLDEN
+    from conftest import oracle_chain_adjoint, oracle_rollout
+    from dexdeform_gb300 import workloads as W
+    from dexdeform_gb300.hand import N_BODIES, SyntheticHand, default_qpos
+    from dexdeform_gb300.torch_wrapper import GradModel
+    hand = SyntheticHand(base_pos=(0.5, 0.2, 0.47), action_scale=0.05)
+    env = W.make_env(11, 20000, "ellipsoid", grid=64, dt=5e-5, center=(0.5, 0.11, 0.5), extent=(0.12, 0.06, 0.09),
+                     nb=N_BODIES, steps=2, name="config1")
+    env.body_tfsr, env.body_args = hand.body_shapes()
+    S, T = 20, 50
+    rng = np.random.default_rng(0)
+    actions = torch.tensor(rng.normal(scale=0.1, size=(S, 24)), dtype=torch.float32, device="cuda")
+    target = torch.tensor(env.x + rng.normal(scale=0.01, size=env.x.shape).astype(np.float32), device="cuda")
+    model = GradModel(env, hand, T, capsule_grad="exact")
+    E = model.sim.E
+    links = []
+    backward = model.sim.backward
+
+    def recording(state, poses, g_out):
+        g_state, g_poses = backward(state, poses, g_out)
+        links.append((state.clone(), poses.clone(), g_out.clone(), g_state.clone(), g_poses.clone()))
+        return g_state, g_poses
+
+    model.sim.backward = recording
+    model.zero_grad()
+    model.reset(default_qpos(), E.pack_state([env.state()]))
+    a = actions.clone().requires_grad_(True)
+    for s in range(S):
+        obs = model.forward(s, a[s])
+    (((obs[0][:, :3].double() - target.double()) ** 2).sum(1).mean()).backward()
+    model.sim.backward = backward
+    assert E.error_word() == 0 and len(links) == S
+    links = links[::-1]  # the backward visits the env steps last to first
+
+    z = np.load(os.path.join(GOLDEN, "ref_batch_adjoint.npz"))
+    fields = [str(f) for f in z["fields"]]
+    bars = {f: max(1e-3, 4.0 * float(z["distance"][:, j].max())) for j, f in enumerate(fields)}
+    oracle_mod.set_capsule_grad("exact")
+    try:
+        for s in range(S):
+            state, poses, g_out, g_state, g_poses = links[s]
+            p = poses.cpu().numpy()
+            env_s = dataclasses.replace(env, poses=np.concatenate([p[..., :3], p[..., 4:]], -1))
+            st = E.unpack_state(state)[0]
+            states = oracle_rollout(oracle_mod, env_s, T, "exact", state=st, storage="fp32")
+            want, bp, br = oracle_chain_adjoint(oracle_mod, env_s, [states[t] for t in range(T + 1)],
+                                                E.unpack_state(g_out)[0], "exact")
+            got = E.unpack_state(g_state)[0]
+            gp = g_poses.cpu().numpy()
+            errs = {k: rel(got[k], want[k]) for k in ("x", "v", "F", "C")}
+            errs["pose_position"], errs["pose_rotation"] = rel(gp[..., :3], bp), rel(gp[..., 4:], br)
+            assert all(errs[f] < bars[f] for f in fields), (s, errs, bars)
+    finally:
+        oracle_mod.set_capsule_grad("reference")
+
+
 @pytest.mark.parametrize("hand_kind", ["synthetic", "shadow"])
 def test_graphed_kinematics_equal_eager(cuda, hand_kind):
     """GradModel with the hand kinematics of each env step replayed as CUDA
