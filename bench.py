@@ -505,12 +505,12 @@ ALG_BYTES = {
 
 
 # DRAM bytes (read + write) per particle of one launch, from ncu captures
-# on the 64-env batch (profiles/k_*_batch64.md; the fused kernels' from the
-# captures of profiles/l2_atomics_batch64.md)
+# on the 64-env batch (654,552 particles, 5 substeps per env step; the fused
+# kernels' on device-sorted input with the segment limit of 12)
 NCU_DRAM_BYTES_PER_PARTICLE = {"p2g_grad": 236.910592e6 / 654552, "g2p2g_tape": 142.285376e6 / 654552,
                                "g2p2g": 63.428544e6 / 654552, "p2g2g_grad": 232.012544e6 / 654552}
 # L2 reduction traffic and the busy fraction of the L2 atomic units of one
-# launch, from an ncu capture on the same batch (profiles/l2_atomics_batch64.md):
+# launch, from an ncu capture on the same batch and input:
 # (lts__t_requests_op_red.sum, lts__t_sectors_op_red.sum,
 #  lts__d_atomic_input_cycles_active.avg.pct_of_peak_sustained_elapsed)
 NCU_L2_RED = {"g2p2g": (2156514, 3752499, 8.13), "g2p2g_tape": (2158644, 3754360, 7.76),
